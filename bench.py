@@ -1,0 +1,405 @@
+#!/usr/bin/env python
+"""Benchmark of the PADO hot path on one GB300: pruned landmark labeling of a
+synthetic graph plus exact distance queries, against the reference's CPU code.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload rmat20|rmat14|wrmat18]
+
+A step labels the whole graph once (bit-parallel rows + every root batch).
+``value`` is canonical labels per second of device labeling time (inputs
+resident in HBM, CUDA events inside the library); ``e2e`` is the same metric
+through the C ABI from pinned host CSR to exported host labels, wall clock.
+Queries (device and host paths), a per-kernel profile pass (roofline), SM clock
+samples and a bounded CPU-baseline sample are reported beside it.  Prints one
+JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+from parallel_distance_oracle_gb300 import graphs as G  # noqa: E402
+
+WORKLOADS = {
+    # configs[1]: unweighted social-like R-MAT, 64 BP roots, batch 1024, 10M queries
+    "rmat20": dict(kind="unw", scale=20, ef=16, seed=2, K=64, B=1024, queries=10_000_000, qseed=12,
+                   desc="R-MAT s20 ef16 (a,b,c=.57,.19,.19), dedup+symmetrised, degree order, K=64, B=1024"),
+    # configs[0]: the CPU-runnable case
+    "rmat14": dict(kind="unw", scale=14, ef=8, seed=1, K=50, B=1024, queries=100_000, qseed=11,
+                   desc="R-MAT s14 ef8, degree order, K=50, B=1024"),
+    # configs[2]: weighted R-MAT, weights 1..100, batch 512
+    "wrmat18": dict(kind="w", scale=18, ef=8, seed=3, K=0, B=512, queries=1_000_000, qseed=13,
+                    desc="weighted R-MAT s18 ef8, weights U[1,100], degree order, B=512"),
+}
+METRIC = "labels_per_s"
+UNIT = "labels/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def ranked_csr(g, rank):
+    """The id_transfer-ed graph (graph.h:176-206): ids are ranks, neighbour
+    lists descending -- what the reference's labeling constructors receive."""
+    src = np.repeat(np.arange(g.n, dtype=np.int64), np.diff(g.off).astype(np.int64))
+    ns = rank[src].astype(np.int64)
+    nd = rank[g.adj].astype(np.int64)
+    order = np.lexsort((-nd, ns))
+    off = np.zeros(g.n + 1, np.uint64)
+    np.cumsum(np.bincount(ns, minlength=g.n), out=off[1:])
+    w = None if g.w is None else g.w[order]
+    return G.CSRGraph(g.n, off, nd[order].astype(np.uint32), w)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sms.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args, wl):
+    """The reference's own CPU labeling (ParaVertexCentricPLL with all host
+    threads when its driver was built here; else the oracle restatement),
+    timed on a bounded sample of the same workload."""
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    from oracle import orc
+    g = gen_graph(wl)
+    rk = G.degree_rank(g)
+    nb = args.ref_batches
+    vals, secs = [], []
+    info = None
+    for i in range(args.warmup + args.steps):
+        r = orc.unw_prefix_sample(g, rk, wl["K"], wl["B"], nb) if wl["kind"] == "unw" else w_prefix(g, rk, wl)
+        if i >= args.warmup:
+            vals.append(r["labels"] / r["seconds"])
+            secs.append(r["seconds"])
+        info = r
+        log(f"reference step {i}: {r['labels']} labels in {r['seconds']:.2f}s ({r['kind']}, {r['cores']} threads)")
+    v = statistics.mean(vals)
+    sample = (f"{wl['desc']}: bit-parallel labeling + first {nb} root batches per step"
+              if wl["kind"] == "unw" else f"{wl['desc']}: full weighted labeling of the sample")
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": statistics.mean(secs) * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u8" if wl["kind"] == "unw" else "int16",
+           "data": "synthetic", "config": {"workload": args.workload, "desc": wl["desc"]},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": info["kind"], "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def w_prefix(g, rk, wl):
+    from oracle import orc
+    t0 = time.perf_counter()
+    if orc.ref_available(50):
+        lab = orc.ref_w_label(g, rk, wl["B"], mode=1, threads=os.cpu_count() or 1)
+        kind, cores = "reference", os.cpu_count() or 1
+        secs = lab.seconds
+    else:
+        lab = orc.w_label(g, rk, wl["B"])
+        kind, cores = "port", 1
+        secs = time.perf_counter() - t0
+    return {"seconds": secs, "labels": len(lab.hub), "kind": kind, "cores": cores}
+
+
+def gen_graph(wl):
+    if wl["kind"] == "unw":
+        return G.rmat(wl["scale"], wl["ef"], wl["seed"])
+    return G.rmat(wl["scale"], wl["ef"], wl["seed"], weights=(1, 100))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS))
+    ap.add_argument("--queries", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-batches", type=int, default=1, help="root batches in one CPU-baseline sample")
+    ap.add_argument("--no-profile", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+
+    import torch
+    world, grank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    from parallel_distance_oracle_gb300 import _lib, pado
+    lib = _lib.lib
+
+    t = time.perf_counter()
+    g = gen_graph(wl)
+    rk = G.degree_rank(g)
+    rg = ranked_csr(g, rk)
+    log(f"graph: n={g.n} m_directed={g.m_directed} ({time.perf_counter() - t:.1f}s to generate and rank)")
+    # pinned host copies of the inputs (the e2e path copies them every step)
+    h_off = torch.from_numpy(rg.off.view(np.int64)).pin_memory()
+    h_adj = torch.from_numpy(rg.adj.view(np.int32)).pin_memory()
+    h_w = torch.from_numpy(rg.w.view(np.uint8)).pin_memory() if rg.w is not None else None
+    h2d = h_off.numel() * 8 + h_adj.numel() * 4 + (h_w.numel() if h_w is not None else 0)
+
+    def build_once():
+        h = C.c_void_p()
+        if wl["kind"] == "unw":
+            _lib.check(lib.pado_unw_build_ranked(g.n, C.c_void_p(h_off.data_ptr()), C.c_void_p(h_adj.data_ptr()),
+                                                 wl["K"], wl["B"], C.byref(h)))
+            idx = pado.VertexCentricPLL()
+        else:
+            _lib.check(lib.pado_w_build_ranked(g.n, C.c_void_p(h_off.data_ptr()), C.c_void_p(h_adj.data_ptr()),
+                                               C.c_void_p(h_w.data_ptr()), wl["B"], C.byref(h)))
+            idx = pado.WeightedVertexCentricPLL()
+        idx._h = h
+        return idx
+
+    out_bufs = {}
+
+    def export(idx):
+        inf = idx.info()
+        n, K, tot = inf.n, inf.bp_roots, inf.num_labels
+        if not out_bufs or out_bufs["tot"] < tot:
+            dsz = 1 if wl["kind"] == "unw" else 2
+            out_bufs.update(tot=tot, off=torch.empty(n + 1, dtype=torch.int64).pin_memory(),
+                            hub=torch.empty(max(tot, 1), dtype=torch.int32).pin_memory(),
+                            dist=torch.empty(max(tot, 1) * dsz, dtype=torch.uint8).pin_memory(),
+                            bpd=torch.empty(max(n * K, 1), dtype=torch.uint8).pin_memory(),
+                            bps=torch.empty(max(n * K * 2, 1), dtype=torch.int64).pin_memory())
+        b = out_bufs
+        _lib.check(lib.pado_export(idx._h, C.c_void_p(b["off"].data_ptr()), C.c_void_p(b["hub"].data_ptr()),
+                                   C.c_void_p(b["dist"].data_ptr()), C.c_void_p(b["bpd"].data_ptr()) if K else None,
+                                   C.c_void_p(b["bps"].data_ptr()) if K else None))
+        dsz = 1 if wl["kind"] == "unw" else 2
+        return (n + 1) * 8 + tot * (4 + dsz) + n * K * 17
+
+    def barrier():
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+
+    for i in range(args.warmup):
+        idx = build_once()
+        export(idx)
+        log(f"warmup {i}: {idx.info().num_labels} labels, device {idx.info().build_seconds:.3f}s")
+        idx.close()
+
+    barrier()
+    launches0 = lib.pado_kernel_launches()
+    dev_s, wall_s, labels, d2h = [], [], 0, 0
+    info = None
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            t0 = time.perf_counter()
+            idx = build_once()
+            d2h = export(idx)
+            t1 = time.perf_counter()
+            info = idx.info()
+            labels = info.num_labels
+            dev_s.append(info.build_seconds)
+            wall_s.append(t1 - t0)
+            log(f"step {i}: labels={labels} device={info.build_seconds:.4f}s (bp {info.bp_seconds:.4f}s) "
+                f"wall={t1 - t0:.3f}s levels={info.levels}")
+            if i < args.steps - 1:
+                idx.close()
+    barrier()
+    launches = lib.pado_kernel_launches() - launches0
+    clocks = clk.summary()
+    dev_mean = statistics.mean(dev_s)
+    wall_mean = statistics.mean(wall_s)
+    if pg:
+        tt = torch.tensor([dev_mean, wall_mean], device="cuda", dtype=torch.float64)
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        dev_mean, wall_mean = tt.tolist()
+
+    # ---- queries on the last index (original ids) ----
+    idx.order_labels(rank=rk)
+    nq = args.queries or wl["queries"]
+    qa, qb = G.random_pairs(g.n, nq, wl["qseed"])
+    da = torch.from_numpy(qa.view(np.int32)).cuda()
+    db = torch.from_numpy(qb.view(np.int32)).cuda()
+    dout = torch.empty(nq, dtype=torch.uint8 if wl["kind"] == "unw" else torch.int16, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        idx.query_device(da.data_ptr(), db.data_ptr(), dout.data_ptr(), nq, stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        idx.query_device(da.data_ptr(), db.data_ptr(), dout.data_ptr(), nq, stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    q_dev_s = e0.elapsed_time(e1) / 1e3 / reps
+    t0 = time.perf_counter()
+    host_out = idx.query(qa, qb)
+    q_e2e_s = time.perf_counter() - t0
+    assert np.array_equal(host_out, dout.cpu().numpy()), "device and host query paths disagree"
+
+    # ---- profile pass: per-kernel device time and algorithmic bytes ----
+    prof = {}
+    if not args.no_profile:
+        _lib.check(lib.pado_profile(1))
+        pidx = build_once()
+        pidx.order_labels(rank=rk)
+        pidx.query_device(da.data_ptr(), db.data_ptr(), dout.data_ptr(), nq, stream.cuda_stream)
+        torch.cuda.synchronize()
+        need = lib.pado_profile_read(None, 0, 0)
+        buf = C.create_string_buffer(need + 16)
+        lib.pado_profile_read(buf, len(buf), 1)
+        _lib.check(lib.pado_profile(0))
+        pidx.close()
+        for ln in buf.value.decode().splitlines():
+            name, launches_k, ms, byts = ln.split()
+            prof[name] = {"launches": int(launches_k), "ms": float(ms), "bytes": int(byts)}
+    peak, peak_src = peaks()
+    roofline = None
+    label_kernels = {k: v for k, v in prof.items() if not k.startswith("query")}
+    if label_kernels:
+        top = max(label_kernels, key=lambda k: label_kernels[k]["ms"])
+        tk = label_kernels[top]
+        tot_ms = sum(v["ms"] for v in label_kernels.values())
+        per_launch_bytes = tk["bytes"] / max(tk["launches"], 1)
+        avg_s = tk["ms"] / 1e3 / max(tk["launches"], 1)
+        ach = per_launch_bytes / avg_s / 1e9 if tk["bytes"] else None
+        roofline = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": (ach / peak) if ach else None, "traffic": traffic_from_profiles(top, args.workload),
+                    "peak_source": peak_src, "share_of_labeling_device_time": tk["ms"] / tot_ms if tot_ms else None,
+                    "launches": tk["launches"], "avg_launch_us": avg_s * 1e6, "bytes_per_launch": per_launch_bytes}
+    qk = "query_unw_kernel" if wl["kind"] == "unw" else "query_w_kernel"
+    q_roof = None
+    if qk in prof and prof[qk]["bytes"]:
+        ach = prof[qk]["bytes"] / (prof[qk]["ms"] / 1e3) / 1e9
+        q_roof = {"kernel": qk, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                  "bytes_per_launch": prof[qk]["bytes"] / prof[qk]["launches"]}
+
+    # ---- CPU baseline (bounded sample) ----
+    cpu = None
+    if not args.no_cpu_baseline and grank == 0:
+        from oracle import orc
+        if wl["kind"] == "unw":
+            r = orc.unw_prefix_sample(g, rk, wl["K"], wl["B"], args.ref_batches)
+            sample = f"bit-parallel labeling + first {args.ref_batches} root batches of the same graph"
+        else:
+            r = w_prefix(g, rk, wl)
+            sample = "full weighted labeling of the same graph"
+        cpu = {"value": r["labels"] / r["seconds"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
+               "sample": sample, "seconds": r["seconds"], "labels": r["labels"]}
+
+    if grank == 0:
+        out = {
+            "metric": METRIC, "value": labels * world / dev_mean, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_mean * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8" if wl["kind"] == "unw" else "int16",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "desc": wl["desc"], "n": g.n, "m_directed": g.m_directed,
+                       "bp_roots": wl["K"], "batch": wl["B"], "l2": "inputs larger than L2 (graph + label state)",
+                       "parallelism": f"replicas x{world}"},
+            "labels": labels, "labeling_s": dev_mean, "bp_s": info.bp_seconds, "levels": info.levels,
+            "e2e": {"value": labels * world / wall_mean, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "wall_s": wall_mean},
+            "queries": {"n": nq, "per_s_device": nq / q_dev_s, "per_s_e2e": nq / q_e2e_s, "roofline": q_roof},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
+            "profile": prof,
+        }
+        print(json.dumps(out), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+def traffic_from_profiles(kernel: str, workload: str):
+    """DRAM bytes per launch for `kernel` from the committed ncu summary
+    (profiles/ncu_traffic.json: {"<workload>:<kernel>": bytes_per_launch})."""
+    p = REPO / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        return json.loads(p.read_text()).get(f"{workload}:{kernel}")
+    except Exception:
+        return None
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,194 @@
+/*
+ * pado_gpu.h -- C ABI of the GB300 PADO library: pruned landmark (2-hop)
+ * labeling and exact distance queries on one GPU.
+ *
+ * The reference (johnpzh/parallel_distance_oracle, "PADO") exposes this path
+ * as C++ class templates whose constructor labels a rank-relabeled Graph and
+ * whose query_distance() answers a pair.  Every entry point below names the
+ * reference interface it replaces; include/pado_gpu.hpp wraps them back into
+ * those class names so pado.cpp / query_distance.cpp compile unchanged.
+ *
+ * Conventions (includes/globals.h:27-40 of the reference):
+ *   vertex ids uint32; unweighted distances uint8 with 255 = unreachable;
+ *   weighted edge weights uint8 (graph.h:300), distances int16 with
+ *   32767 = unreachable.
+ *   "rank" arrays follow Graph::id_transfer (graph.h:176-206): rank[v] is the
+ *   position of original vertex v in the vertex order, 0 = most important.
+ *   Query endpoints are ORIGINAL ids (as after order_labels() /
+ *   load_index_from_file() in the reference); a hub id in an exported label is
+ *   a RANK, exactly like the reference's Index.
+ *
+ * All functions return a pado_status; pado_last_error() gives the message of
+ * the most recent failure on the calling thread.  No function exits the
+ * process.  One GPU: the device current on the calling thread when the index
+ * is created is used for its whole life.  An index may be queried from
+ * several host threads at once; building, loading and freeing are
+ * single-owner.
+ */
+#ifndef PADO_GPU_H_
+#define PADO_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pado_status {
+    PADO_OK = 0,
+    PADO_E_ARG = 1,       /* invalid argument (sizes, ids, batch size, ...) */
+    PADO_E_NOMEM = 2,     /* device or host allocation failed */
+    PADO_E_CUDA = 3,      /* a CUDA call failed */
+    PADO_E_OVERFLOW = 4,  /* a distance does not fit the reference's type
+                             (unweighted BFS level >= 255) */
+    PADO_E_IO = 5,        /* index file could not be read or written */
+    PADO_E_TIMEOUT = 6,   /* a bounded device wait gave up */
+    PADO_E_STATE = 7      /* call not valid for this index (e.g. weighted vs
+                             unweighted) */
+} pado_status;
+
+typedef struct pado_index pado_index;
+
+/* Label set kind. */
+#define PADO_UNWEIGHTED 0
+#define PADO_WEIGHTED 1
+
+/* Maximum bit-parallel roots and root batch size the kernels accept. */
+#define PADO_MAX_BP_ROOTS 64u
+#define PADO_MAX_BATCH 2048u
+
+const char *pado_last_error(void);
+const char *pado_status_string(int status);
+/* Library version string, e.g. "pado-gpu 0.1 sm_103a". */
+const char *pado_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Building.
+ *
+ * pado_unw_build replaces the labeling constructor
+ *   VertexCentricPLL<BATCH_SIZE>::VertexCentricPLL(const Graph &G)
+ *     (includes/pado_unw_unv_unp.h:260-264, construct :990-1118)
+ *   ParaVertexCentricPLL<BATCH_SIZE>::ParaVertexCentricPLL(const Graph &G)
+ *     (includes/pado_unw_unv_para.201912311607.parallel_bp_labeling.h:307-311)
+ * extended, as the rebuild's interface asks, with the vertex order, the
+ * bit-parallel root count (a class constant, 50, in the reference:
+ * pado_unw_unv_unp.h:46) and the root batch size (the BATCH_SIZE template
+ * argument).
+ *
+ * The graph is an undirected CSR over ORIGINAL ids with both directions
+ * stored: off[n+1] (off[n] = number of directed entries), adj[off[n]].
+ * Duplicate entries are kept and self-loops are honoured exactly as the
+ * reference's Graph does (graph.h:125-153).  rank[n] is the vertex order.
+ * bp_roots <= 64, 1 <= batch <= 2048.
+ * ------------------------------------------------------------------------- */
+int pado_unw_build(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint32_t *rank,
+                   uint32_t bp_roots, uint32_t batch, pado_index **out);
+
+/* Same, for a graph that is ALREADY rank-relabeled (ids are ranks), which is
+ * what the reference's constructors receive after Graph::id_transfer().  The
+ * neighbour lists need not be sorted.  Query endpoints are ranks until
+ * pado_set_order() installs the original-id mapping (order_labels,
+ * pado_unw_unv_unp.h:1227-1310). */
+int pado_unw_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, uint32_t bp_roots,
+                          uint32_t batch, pado_index **out);
+
+/* Weighted labeling; replaces
+ *   WeightedVertexCentricPLL<BATCH_SIZE>::WeightedVertexCentricPLL(const WeightedGraph &)
+ *     (includes/pado_weighted_unv_unp.h:275-279, construct :1408-1526)
+ *   WeightedParaVertexCentricPLL<BATCH_SIZE>::WeightedParaVertexCentricPLL(...)
+ *     (includes/pado_weighted_unv_para.h:296-300).
+ * w[off[n]] are the per-entry edge weights (uint8, as WeightedGraph stores
+ * them). */
+int pado_w_build(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w,
+                 const uint32_t *rank, uint32_t batch, pado_index **out);
+int pado_w_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w,
+                        uint32_t batch, pado_index **out);
+
+/* Install the original-id mapping (rank[v] = rank of original vertex v).
+ * Replaces order_labels(rank2id, rank) (pado_unw_unv_unp.h:1227-1310,
+ * pado_weighted_unv_unp.h:1715-1779) for indexes built from ranked graphs. */
+int pado_set_order(pado_index *h, const uint32_t *rank);
+
+void pado_free(pado_index *h);
+
+/* ---------------------------------------------------------------------------
+ * Introspection and export (canonical form = the reference's Index after
+ * order_labels: per ORIGINAL vertex, its (rank hub, distance) labels sorted by
+ * hub, plus for unweighted indexes the bp_roots bit-parallel rows).
+ * ------------------------------------------------------------------------- */
+typedef struct pado_info {
+    uint32_t n;
+    uint32_t kind;        /* PADO_UNWEIGHTED or PADO_WEIGHTED */
+    uint32_t bp_roots;
+    uint32_t batch;
+    uint64_t num_labels;  /* total normal labels (canonical) */
+    double build_seconds; /* device time of the labeling (BP + batches) */
+    double bp_seconds;    /* device time of the bit-parallel labeling */
+    uint64_t device_bytes;/* device memory held by the index */
+    uint32_t levels;      /* BFS levels / relaxation rounds run */
+    uint32_t batches;
+} pado_info;
+
+int pado_get_info(const pado_index *h, pado_info *info);
+
+/* Host buffers: off[n+1], hub[num_labels], dist[num_labels] (uint8 for
+ * unweighted, int16 for weighted), bp_dist[n*bp_roots] and
+ * bp_sets[n*bp_roots*2] (S^-1, S^0 per root; unweighted only, may be NULL). */
+int pado_export(const pado_index *h, uint64_t *off, uint32_t *hub, void *dist, uint8_t *bp_dist,
+                uint64_t *bp_sets);
+
+/* Create a query-only index from canonical arrays (e.g. labels produced by
+ * the reference); the inverse of pado_export. */
+int pado_import(uint32_t kind, uint32_t n, uint32_t bp_roots, const uint64_t *off, const uint32_t *hub,
+                const void *dist, const uint8_t *bp_dist, const uint64_t *bp_sets, pado_index **out);
+
+/* ---------------------------------------------------------------------------
+ * Queries; replace query_distance(a, b)
+ *   (pado_unw_unv_unp.h:1312-1445 -> uint8, pado_weighted_unv_unp.h:1782-1900
+ *   -> int16).  Out-of-range ids give 0 when a == b, else unreachable.
+ * ------------------------------------------------------------------------- */
+/* Host arrays: a[k], b[k], out[k] (uint8_t for unweighted, int16_t for
+ * weighted).  Synchronous. */
+int pado_query(pado_index *h, uint64_t k, const uint32_t *a, const uint32_t *b, void *out);
+
+/* Device arrays, enqueued on `stream` (a cudaStream_t, 0 = legacy default);
+ * returns once enqueued. */
+int pado_query_device(pado_index *h, uint64_t k, const uint32_t *d_a, const uint32_t *d_b,
+                      void *d_out, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Index files, in the reference's on-disk format:
+ *   store_index_to_file (pado_unw_unv_unp.h:1120-1180,
+ *                        pado_weighted_unv_unp.h:1639-1676)
+ *   load_index_from_file (pado_unw_unv_unp.h:1182-1224,
+ *                         pado_weighted_unv_unp.h:1678-1711)
+ * Unweighted: [n u32][K u32] then per original vertex K x (u8 d, u64 S^-1,
+ * u64 S^0), u32 count, count x (u32 hub, u8 d).  Weighted: [n u32] then per
+ * vertex u32 count, count x (u32 hub, i16 d).
+ * ------------------------------------------------------------------------- */
+int pado_store(const pado_index *h, const char *path);
+int pado_load(const char *path, uint32_t kind, pado_index **out);
+
+/* ---------------------------------------------------------------------------
+ * Accounting (no counterpart in the reference, which prints wall-clock
+ * timers such as Total_labeling_time, pado_unw_unv_unp.h:1000-1116).
+ * ------------------------------------------------------------------------- */
+/* Kernel launches this library has made in the process so far. */
+uint64_t pado_kernel_launches(void);
+
+/* Enable (1) or disable (0) per-kernel timing: while enabled every launch is
+ * bracketed by CUDA events on its stream and hot kernels count their
+ * algorithmic bytes.  Adds overhead; for profiling runs only. */
+int pado_profile(int enable);
+
+/* Write the profile table as text lines "kernel launches total_ms bytes" into
+ * buf (NUL-terminated, truncated to len); returns the size needed.  reset != 0
+ * clears the table afterwards.  Synchronizes the device. */
+size_t pado_profile_read(char *buf, size_t len, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PADO_GPU_H_ */

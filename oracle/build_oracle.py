@@ -1,0 +1,127 @@
+"""Build recipe for the test oracle (TEST INFRASTRUCTURE ONLY).
+
+Two products, both git-ignored build outputs:
+
+* ``oracle/liboracle.so`` -- the CPU restatement in ``pado_oracle.cpp``.  Always
+  built (here and on the GPU host); the tests, the smoke check and the bench's
+  CPU-baseline leg load it through ctypes.
+* ``oracle/_ref/libpado_ref_k{50,64}.so`` -- the reference's own labeler
+  classes, driven by ``ref_driver.cpp``.  The reference headers do not compile
+  with GCC as shipped (missing ``typename`` on dependent constructor calls,
+  x86-only intrinsic headers), so ``stage_reference()`` writes a mechanically
+  patched copy of the six headers the driver needs into ``oracle/_ref/inc``
+  (never committed).  The patches change no algorithm:
+    1. ``IndexType::Batch(`` / ``IndexType::DistanceIndexType(`` gain
+       ``typename``;
+    2. the ``<xmmintrin.h>``/``<immintrin.h>`` includes are dropped (the
+       force-included ``ref_prelude.h`` supplies them on x86 and stand-ins
+       elsewhere);
+    3. the class constant ``BITPARALLEL_SIZE = 50`` becomes the macro
+       ``PADO_REF_BP_SIZE`` so that the 64-root configuration can be built.
+  Staging needs the reference tree (``PADO_REFERENCE_DIR``, default: the
+  mounted reference); compiling only needs the staged copy, so a host that
+  received ``oracle/_ref/inc`` can build the driver without the tree.
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+from pathlib import Path
+
+ORACLE_DIR = Path(__file__).resolve().parent
+REF_OUT = ORACLE_DIR / "_ref"
+REF_INC = REF_OUT / "inc"
+PORT_SO = ORACLE_DIR / "liboracle.so"
+
+REF_HEADERS = [
+    "globals.h",
+    "graph.h",
+    "pado_unw_unv_unp.h",
+    "pado_unw_unv_para.201912311607.parallel_bp_labeling.h",
+    "pado_weighted_unv_unp.h",
+    "pado_weighted_unv_para.h",
+]
+REF_BP_SIZES = (50, 64)
+
+
+def _reference_dir() -> Path:
+    return Path(os.environ.get("PADO_REFERENCE_DIR", "/root/reference"))
+
+
+def _newer(out: Path, *inputs: Path) -> bool:
+    if not out.exists():
+        return False
+    t = out.stat().st_mtime
+    return all(p.stat().st_mtime <= t for p in inputs if p.exists())
+
+
+def build_port(force: bool = False) -> Path:
+    src = ORACLE_DIR / "pado_oracle.cpp"
+    if force or not _newer(PORT_SO, src):
+        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", str(src), "-o", str(PORT_SO)]
+        subprocess.run(cmd, check=True)
+    return PORT_SO
+
+
+_TYPENAME_RE = re.compile(r"([^a-zA-Z_:])IndexType::(Batch|DistanceIndexType)\(")
+
+
+def _patch(text: str) -> str:
+    text = _TYPENAME_RE.sub(r"\1typename IndexType::\2(", text)
+    text = re.sub(r"^\s*#include\s*<(xmmintrin|immintrin)\.h>\s*$", "", text, flags=re.M)
+    text = text.replace("static const inti BITPARALLEL_SIZE = 50;",
+                        "static const inti BITPARALLEL_SIZE = PADO_REF_BP_SIZE;")
+    return text
+
+
+def stage_reference() -> bool:
+    """Write the patched header copy into oracle/_ref/inc.  False if no tree."""
+    src = _reference_dir() / "includes"
+    if not src.is_dir():
+        return False
+    REF_INC.mkdir(parents=True, exist_ok=True)
+    for name in REF_HEADERS:
+        out = REF_INC / name
+        text = _patch((src / name).read_text(errors="replace"))
+        if not out.exists() or out.read_text(errors="replace") != text:
+            out.write_text(text)
+    return True
+
+
+def ref_so(k: int) -> Path:
+    return REF_OUT / f"libpado_ref_k{k}.so"
+
+
+def build_reference(force: bool = False, sizes=REF_BP_SIZES) -> list[Path]:
+    """Compile the reference driver for each BP size.  [] if not staged."""
+    stage_reference()
+    if not all((REF_INC / h).exists() for h in REF_HEADERS):
+        return []
+    deps = [ORACLE_DIR / "ref_driver.cpp", ORACLE_DIR / "ref_prelude.h"] + [REF_INC / h for h in REF_HEADERS]
+    procs = []
+    outs = []
+    for k in sizes:
+        out = ref_so(k)
+        outs.append(out)
+        if not force and _newer(out, *deps):
+            continue
+        cmd = ["g++", "-std=c++14", "-O3", "-fopenmp", "-fPIC", "-shared", "-w",
+               f"-DPADO_REF_BP_SIZE={k}", "-I", str(REF_INC), "-I", str(ORACLE_DIR),
+               str(ORACLE_DIR / "ref_driver.cpp"), "-o", str(out)]
+        procs.append((cmd, subprocess.Popen(cmd)))
+    for cmd, p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("reference driver build failed: " + " ".join(cmd))
+    return outs
+
+
+def build_all() -> None:
+    build_port()
+    build_reference()
+
+
+if __name__ == "__main__":
+    build_all()
+    print("oracle:", PORT_SO, "reference:", [str(p) for p in build_reference()], file=sys.stderr)

@@ -1,0 +1,89 @@
+"""ctypes binding of include/pado_gpu.h (libpado_gpu.so, built in-tree).
+
+There is no CPU fallback: if the CUDA library is missing or fails to load,
+importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+PADO_OK = 0
+PADO_UNWEIGHTED = 0
+PADO_WEIGHTED = 1
+
+
+class PadoError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class Info(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("kind", C.c_uint32), ("bp_roots", C.c_uint32), ("batch", C.c_uint32),
+                ("num_labels", C.c_uint64), ("build_seconds", C.c_double), ("bp_seconds", C.c_double),
+                ("device_bytes", C.c_uint64), ("levels", C.c_uint32), ("batches", C.c_uint32)]
+
+
+def _load() -> C.CDLL:
+    lib_path: Path = _build.LIB
+    if not _build.up_to_date():
+        try:
+            _build.build()
+        except Exception as e:  # no toolchain: a stale library is still usable
+            if not lib_path.exists():
+                raise ImportError(f"libpado_gpu.so is not built and cannot be built: {e}") from e
+    lib = C.CDLL(str(lib_path))
+    vp = C.c_void_p
+    u32, u64 = C.c_uint32, C.c_uint64
+    P = C.POINTER
+    sig = {
+        "pado_last_error": (C.c_char_p, []),
+        "pado_status_string": (C.c_char_p, [C.c_int]),
+        "pado_version": (C.c_char_p, []),
+        "pado_unw_build": (C.c_int, [u32, vp, vp, vp, u32, u32, P(vp)]),
+        "pado_unw_build_ranked": (C.c_int, [u32, vp, vp, u32, u32, P(vp)]),
+        "pado_w_build": (C.c_int, [u32, vp, vp, vp, vp, u32, P(vp)]),
+        "pado_w_build_ranked": (C.c_int, [u32, vp, vp, vp, u32, P(vp)]),
+        "pado_set_order": (C.c_int, [vp, vp]),
+        "pado_free": (None, [vp]),
+        "pado_get_info": (C.c_int, [vp, P(Info)]),
+        "pado_export": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+        "pado_import": (C.c_int, [u32, u32, u32, vp, vp, vp, vp, vp, P(vp)]),
+        "pado_query": (C.c_int, [vp, u64, vp, vp, vp]),
+        "pado_query_device": (C.c_int, [vp, u64, vp, vp, vp, vp]),
+        "pado_store": (C.c_int, [vp, C.c_char_p]),
+        "pado_load": (C.c_int, [C.c_char_p, u32, P(vp)]),
+        "pado_kernel_launches": (u64, []),
+        "pado_profile": (C.c_int, [C.c_int]),
+        "pado_profile_read": (C.c_size_t, [C.c_char_p, C.c_size_t, C.c_int]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+lib = _load()
+
+# Every symbol include/pado_gpu.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "pado_last_error", "pado_status_string", "pado_version", "pado_unw_build", "pado_unw_build_ranked",
+    "pado_w_build", "pado_w_build_ranked", "pado_set_order", "pado_free", "pado_get_info", "pado_export",
+    "pado_import", "pado_query", "pado_query_device", "pado_store", "pado_load", "pado_kernel_launches",
+    "pado_profile", "pado_profile_read",
+]
+
+
+def check(status: int) -> None:
+    if status != PADO_OK:
+        raise PadoError(status, lib.pado_last_error().decode(errors="replace"))
+
+
+def ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)

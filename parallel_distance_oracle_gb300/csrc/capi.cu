@@ -1,0 +1,521 @@
+// capi.cu -- the C ABI (include/pado_gpu.h): index handles, host-side graph
+// relabeling, export/import, queries and the reference's index file format.
+
+#include <algorithm>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <thread>
+
+#include "pado_internal.cuh"
+
+struct pado_index {
+    uint32_t kind = PADO_UNWEIGHTED;
+    uint32_t n = 0, K = 0, B = 0;
+    int device = 0;
+    pado::DBuf<uint32_t> rank;   // original id -> rank (empty: identity)
+    pado::LabelStore store;      // rank-indexed canonical labels
+    pado::DBuf<uint8_t> bpd;     // n * K, rank-indexed
+    pado::DBuf<uint64_t> bps;    // n * K * 2
+    pado_info info{};
+
+    pado::IndexView view() const
+    {
+        pado::IndexView v;
+        v.n = n;
+        v.K = K;
+        v.rank = rank.n ? rank.p : nullptr;
+        v.off = store.off.p;
+        v.hub = store.hub.p;
+        v.dist8 = store.dist8.p;
+        v.dist16 = store.dist16.p;
+        v.bpd = bpd.p;
+        v.bps = bps.p;
+        return v;
+    }
+    uint64_t device_bytes() const
+    {
+        return rank.bytes() + store.off.bytes() + store.hub.bytes() + store.dist8.bytes() + store.dist16.bytes() +
+               bpd.bytes() + bps.bytes();
+    }
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+template <typename F>
+int guarded(F &&f)
+{
+    try {
+        f();
+        return PADO_OK;
+    } catch (const pado::Error &e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(PADO_E_NOMEM, "host allocation failed");
+    } catch (const std::exception &e) {
+        return fail(PADO_E_CUDA, e.what());
+    }
+}
+
+// Run f(lo, hi) over [0, n) on the host's cores (plain threads, no OpenMP).
+template <typename F>
+void parallel_ranges(uint32_t n, F &&f)
+{
+    unsigned T = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    if (n < 4096 || T == 1) {
+        f(0u, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (unsigned i = 0; i < T; ++i) {
+        uint32_t lo = (uint32_t)((uint64_t)n * i / T), hi = (uint32_t)((uint64_t)n * (i + 1) / T);
+        th.emplace_back([&, lo, hi] { f(lo, hi); });
+    }
+    for (auto &t : th) t.join();
+}
+
+void check_graph(uint32_t n, const uint64_t *off, const uint32_t *adj)
+{
+    PADO_CHECK(off != nullptr, PADO_E_ARG, "null offsets");
+    PADO_CHECK(off[0] == 0, PADO_E_ARG, "off[0] must be 0");
+    for (uint32_t v = 0; v < n; ++v) PADO_CHECK(off[v + 1] >= off[v], PADO_E_ARG, "offsets must be non-decreasing");
+    PADO_CHECK(off[n] < (1ull << 32), PADO_E_ARG, "more than 2^32-1 adjacency entries");
+    PADO_CHECK(off[n] == 0 || adj != nullptr, PADO_E_ARG, "null adjacency");
+    for (uint64_t e = 0; e < off[n]; ++e) PADO_CHECK(adj[e] < n, PADO_E_ARG, "adjacency id out of range");
+}
+
+void check_rank(uint32_t n, const uint32_t *rank)
+{
+    PADO_CHECK(rank != nullptr || n == 0, PADO_E_ARG, "null rank");
+    std::vector<uint8_t> seen(n, 0);
+    for (uint32_t v = 0; v < n; ++v) {
+        PADO_CHECK(rank[v] < n && !seen[rank[v]], PADO_E_ARG, "rank is not a permutation of 0..n-1");
+        seen[rank[v]] = 1;
+    }
+}
+
+void upload_graph(const pado::HostGraph &hg, pado::DevGraph &g, bool weighted, cudaStream_t s)
+{
+    g.n = hg.n;
+    g.m = hg.adj.size();
+    g.off.alloc(hg.n + 1);
+    g.off.upload(hg.off.data(), hg.n + 1, s);
+    g.adj.alloc(std::max<uint64_t>(g.m, 1));
+    g.adj.upload(hg.adj.data(), g.m, s);
+    if (weighted) {
+        g.w.alloc(std::max<uint64_t>(g.m, 1));
+        g.w.upload(hg.w.data(), g.m, s);
+    }
+}
+
+int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w,
+                 const uint32_t *rank, uint32_t K, uint32_t B, pado_index **out)
+{
+    if (!out) return fail(PADO_E_ARG, "null output handle");
+    *out = nullptr;
+    return guarded([&] {
+        PADO_CHECK(B >= 1 && B <= pado::MAX_BATCH, PADO_E_ARG, "batch size must be in [1, 2048]");
+        PADO_CHECK(K <= pado::MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
+        PADO_CHECK(!weighted || w != nullptr || (off && off[n] == 0), PADO_E_ARG, "null weights");
+        check_graph(n, off, adj);
+        if (rank) check_rank(n, rank);
+        std::unique_ptr<pado_index> h(new pado_index);
+        PADO_CUDA(cudaGetDevice(&h->device));
+        h->kind = weighted ? PADO_WEIGHTED : PADO_UNWEIGHTED;
+        h->n = n;
+        h->K = weighted ? 0 : K;
+        h->B = B;
+        cudaStream_t s;
+        PADO_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
+        pado::HostGraph hg = pado::relabel_host(n, off, adj, weighted ? w : nullptr, rank);
+        pado::DevGraph g;
+        upload_graph(hg, g, weighted, s);
+        if (rank) {
+            h->rank.alloc(std::max<uint32_t>(n, 1));
+            h->rank.upload(rank, n, s);
+        }
+        pado::LabelRun run;
+        if (!weighted) {
+            std::vector<uint8_t> used(n, 0);
+            h->bpd.alloc(std::max<uint64_t>((uint64_t)n * K, 1));
+            h->bps.alloc(std::max<uint64_t>((uint64_t)n * K * 2, 1));
+            pado::BpResult bp = pado::bp_label(hg, g, K, used, h->bpd.p, h->bps.p, s);
+            run = pado::unw_label(g, K, B, used, h->bpd.p, h->bps.p, h->store, s);
+            h->info.bp_seconds = bp.ms * 1e-3;
+            h->info.build_seconds = (bp.ms + run.ms) * 1e-3;
+            h->info.levels = run.levels + bp.levels;
+        } else {
+            run = pado::w_label(g, B, h->store, s);
+            h->info.build_seconds = run.ms * 1e-3;
+            h->info.levels = run.levels;
+        }
+        PADO_CUDA(cudaStreamSynchronize(s));
+        h->info.n = n;
+        h->info.kind = h->kind;
+        h->info.bp_roots = h->K;
+        h->info.batch = B;
+        h->info.num_labels = h->store.total;
+        h->info.batches = run.batches;
+        h->info.device_bytes = h->device_bytes();
+        *out = h.release();
+    });
+}
+
+}  // namespace
+
+namespace pado {
+
+HostGraph relabel_host(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, const uint32_t *rank)
+{
+    HostGraph g;
+    g.n = n;
+    g.off.assign(n + 1, 0);
+    const uint64_t m = off[n];
+    g.adj.resize(m);
+    if (w) g.w.resize(m);
+    if (rank) {
+        for (uint32_t v = 0; v < n; ++v) g.off[rank[v] + 1] = (uint32_t)(off[v + 1] - off[v]);
+        for (uint32_t v = 0; v < n; ++v) g.off[v + 1] += g.off[v];
+    } else {
+        for (uint32_t v = 0; v <= n; ++v) g.off[v] = (uint32_t)off[v];
+    }
+    parallel_ranges(n, [&](uint32_t lo, uint32_t hi) {
+        std::vector<std::pair<uint32_t, uint8_t>> tmp;
+        for (uint32_t v = lo; v < hi; ++v) {
+            const uint32_t nv = rank ? rank[v] : v;
+            const uint64_t b = off[v], e = off[v + 1];
+            uint32_t *dst = g.adj.data() + g.off[nv];
+            uint8_t *dw = w ? g.w.data() + g.off[nv] : nullptr;
+            bool sorted = true;
+            for (uint64_t k = b; k < e; ++k) {
+                const uint32_t x = rank ? rank[adj[k]] : adj[k];
+                dst[k - b] = x;
+                if (dw) dw[k - b] = w[k];
+                if (k > b) {
+                    const uint32_t y = dst[k - b - 1];
+                    if (y < x || (y == x && dw && dw[k - b - 1] < dw[k - b])) sorted = false;
+                }
+            }
+            if (sorted) continue;
+            // descending (id, weight), as Graph::id_transfer sorts (graph.h:192, :389)
+            tmp.resize(e - b);
+            for (uint64_t k = 0; k < e - b; ++k) tmp[k] = {dst[k], dw ? dw[k] : (uint8_t)0};
+            std::sort(tmp.rbegin(), tmp.rend());
+            for (uint64_t k = 0; k < e - b; ++k) {
+                dst[k] = tmp[k].first;
+                if (dw) dw[k] = tmp[k].second;
+            }
+        }
+    });
+    return g;
+}
+
+}  // namespace pado
+
+extern "C" {
+
+const char *pado_last_error(void) { return g_err.c_str(); }
+
+const char *pado_status_string(int status)
+{
+    switch (status) {
+    case PADO_OK: return "ok";
+    case PADO_E_ARG: return "invalid argument";
+    case PADO_E_NOMEM: return "out of memory";
+    case PADO_E_CUDA: return "CUDA error";
+    case PADO_E_OVERFLOW: return "distance overflow";
+    case PADO_E_IO: return "I/O error";
+    case PADO_E_TIMEOUT: return "device wait timed out";
+    case PADO_E_STATE: return "invalid state";
+    default: return "unknown status";
+    }
+}
+
+const char *pado_version(void) { return "pado-gpu 0.1 sm_103a"; }
+
+int pado_unw_build(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint32_t *rank, uint32_t bp_roots,
+                   uint32_t batch, pado_index **out)
+{
+    if (!rank && n) return fail(PADO_E_ARG, "null rank");
+    return build_common(false, n, off, adj, nullptr, rank, bp_roots, batch, out);
+}
+
+int pado_unw_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, uint32_t bp_roots, uint32_t batch,
+                          pado_index **out)
+{
+    return build_common(false, n, off, adj, nullptr, nullptr, bp_roots, batch, out);
+}
+
+int pado_w_build(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, const uint32_t *rank,
+                 uint32_t batch, pado_index **out)
+{
+    if (!rank && n) return fail(PADO_E_ARG, "null rank");
+    return build_common(true, n, off, adj, w, rank, 0, batch, out);
+}
+
+int pado_w_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, uint32_t batch,
+                        pado_index **out)
+{
+    return build_common(true, n, off, adj, w, nullptr, 0, batch, out);
+}
+
+int pado_set_order(pado_index *h, const uint32_t *rank)
+{
+    if (!h) return fail(PADO_E_ARG, "null index");
+    return guarded([&] {
+        check_rank(h->n, rank);
+        PADO_CUDA(cudaSetDevice(h->device));
+        h->rank.alloc(std::max<uint32_t>(h->n, 1));
+        h->rank.upload(rank, h->n, 0);
+        PADO_CUDA(cudaDeviceSynchronize());
+        h->info.device_bytes = h->device_bytes();
+    });
+}
+
+void pado_free(pado_index *h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    delete h;
+}
+
+int pado_get_info(const pado_index *h, pado_info *info)
+{
+    if (!h || !info) return fail(PADO_E_ARG, "null argument");
+    *info = h->info;
+    return PADO_OK;
+}
+
+int pado_export(const pado_index *h, uint64_t *off, uint32_t *hub, void *dist, uint8_t *bp_dist, uint64_t *bp_sets)
+{
+    if (!h || !off || (h->store.total && (!hub || !dist))) return fail(PADO_E_ARG, "null argument");
+    return guarded([&] {
+        PADO_CUDA(cudaSetDevice(h->device));
+        const uint32_t n = h->n, K = h->K;
+        const size_t dsz = h->kind == PADO_WEIGHTED ? 2 : 1;
+        std::vector<uint64_t> roff(n + 1);
+        std::vector<uint32_t> rhub(h->store.total);
+        std::vector<uint8_t> rdist(h->store.total * dsz);
+        h->store.off.download(roff.data(), n + 1);
+        h->store.hub.download(rhub.data(), h->store.total);
+        if (dsz == 1)
+            h->store.dist8.download(rdist.data(), h->store.total);
+        else
+            h->store.dist16.download(reinterpret_cast<int16_t *>(rdist.data()), h->store.total);
+        std::vector<uint32_t> rk;
+        if (h->rank.n) {
+            rk.resize(n);
+            h->rank.download(rk.data(), n);
+        }
+        std::vector<uint8_t> rbpd;
+        std::vector<uint64_t> rbps;
+        if (K && (bp_dist || bp_sets)) {
+            rbpd.resize((size_t)n * K);
+            rbps.resize((size_t)n * K * 2);
+            h->bpd.download(rbpd.data(), rbpd.size());
+            h->bps.download(rbps.data(), rbps.size());
+        }
+        PADO_CUDA(cudaDeviceSynchronize());
+        off[0] = 0;
+        for (uint32_t v = 0; v < n; ++v) {
+            const uint32_t r = rk.empty() ? v : rk[v];
+            const uint64_t b = roff[r], len = roff[r + 1] - b;
+            off[v + 1] = off[v] + len;
+            if (len) {
+                memcpy(hub + off[v], rhub.data() + b, len * 4);
+                memcpy(static_cast<uint8_t *>(dist) + off[v] * dsz, rdist.data() + b * dsz, len * dsz);
+            }
+            if (K && bp_dist) memcpy(bp_dist + (size_t)v * K, rbpd.data() + (size_t)r * K, K);
+            if (K && bp_sets) memcpy(bp_sets + (size_t)v * K * 2, rbps.data() + (size_t)r * K * 2, K * 16);
+        }
+    });
+}
+
+int pado_import(uint32_t kind, uint32_t n, uint32_t bp_roots, const uint64_t *off, const uint32_t *hub, const void *dist,
+                const uint8_t *bp_dist, const uint64_t *bp_sets, pado_index **out)
+{
+    if (!out || !off) return fail(PADO_E_ARG, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        PADO_CHECK(kind == PADO_UNWEIGHTED || kind == PADO_WEIGHTED, PADO_E_ARG, "unknown index kind");
+        PADO_CHECK(bp_roots <= pado::MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
+        PADO_CHECK(kind == PADO_UNWEIGHTED || bp_roots == 0, PADO_E_ARG, "weighted indexes have no BP roots");
+        PADO_CHECK(bp_roots == 0 || (bp_dist && bp_sets), PADO_E_ARG, "null bit-parallel rows");
+        PADO_CHECK(off[0] == 0, PADO_E_ARG, "off[0] must be 0");
+        for (uint32_t v = 0; v < n; ++v) PADO_CHECK(off[v + 1] >= off[v], PADO_E_ARG, "offsets must be non-decreasing");
+        const uint64_t tot = off[n];
+        PADO_CHECK(tot == 0 || (hub && dist), PADO_E_ARG, "null labels");
+        for (uint32_t v = 0; v < n; ++v)
+            for (uint64_t j = off[v]; j < off[v + 1]; ++j) {
+                PADO_CHECK(hub[j] < n, PADO_E_ARG, "hub id out of range");
+                PADO_CHECK(j == off[v] || hub[j - 1] < hub[j], PADO_E_ARG, "labels must be sorted by hub, unique");
+            }
+        std::unique_ptr<pado_index> h(new pado_index);
+        PADO_CUDA(cudaGetDevice(&h->device));
+        h->kind = kind;
+        h->n = n;
+        h->K = bp_roots;
+        h->store.total = tot;
+        h->store.off.alloc(n + 1);
+        h->store.off.upload(off, n + 1);
+        h->store.hub.alloc(std::max<uint64_t>(tot, 1));
+        h->store.hub.upload(hub, tot);
+        if (kind == PADO_UNWEIGHTED) {
+            h->store.dist8.alloc(std::max<uint64_t>(tot, 1));
+            h->store.dist8.upload(static_cast<const uint8_t *>(dist), tot);
+        } else {
+            h->store.dist16.alloc(std::max<uint64_t>(tot, 1));
+            h->store.dist16.upload(static_cast<const int16_t *>(dist), tot);
+        }
+        if (bp_roots) {
+            h->bpd.alloc((uint64_t)n * bp_roots);
+            h->bpd.upload(bp_dist, (uint64_t)n * bp_roots);
+            h->bps.alloc((uint64_t)n * bp_roots * 2);
+            h->bps.upload(bp_sets, (uint64_t)n * bp_roots * 2);
+        }
+        PADO_CUDA(cudaDeviceSynchronize());
+        h->info.n = n;
+        h->info.kind = kind;
+        h->info.bp_roots = bp_roots;
+        h->info.num_labels = tot;
+        h->info.device_bytes = h->device_bytes();
+        *out = h.release();
+    });
+}
+
+int pado_query_device(pado_index *h, uint64_t k, const uint32_t *d_a, const uint32_t *d_b, void *d_out, void *stream)
+{
+    if (!h || (k && (!d_a || !d_b || !d_out))) return fail(PADO_E_ARG, "null argument");
+    return guarded([&] {
+        PADO_CUDA(cudaSetDevice(h->device));
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (h->kind == PADO_UNWEIGHTED)
+            pado::launch_query_unw(h->view(), k, d_a, d_b, static_cast<uint8_t *>(d_out), s);
+        else
+            pado::launch_query_w(h->view(), k, d_a, d_b, static_cast<int16_t *>(d_out), s);
+    });
+}
+
+int pado_query(pado_index *h, uint64_t k, const uint32_t *a, const uint32_t *b, void *out)
+{
+    if (!h || (k && (!a || !b || !out))) return fail(PADO_E_ARG, "null argument");
+    if (!k) return PADO_OK;
+    return guarded([&] {
+        PADO_CUDA(cudaSetDevice(h->device));
+        cudaStream_t s = cudaStreamPerThread;
+        const size_t osz = h->kind == PADO_UNWEIGHTED ? 1 : 2;
+        void *buf = nullptr;
+        PADO_CUDA(cudaMallocAsync(&buf, k * (8 + osz), s));
+        uint32_t *da = static_cast<uint32_t *>(buf), *db = da + k;
+        void *dout = db + k;
+        try {
+            PADO_CUDA(cudaMemcpyAsync(da, a, k * 4, cudaMemcpyHostToDevice, s));
+            PADO_CUDA(cudaMemcpyAsync(db, b, k * 4, cudaMemcpyHostToDevice, s));
+            if (h->kind == PADO_UNWEIGHTED)
+                pado::launch_query_unw(h->view(), k, da, db, static_cast<uint8_t *>(dout), s);
+            else
+                pado::launch_query_w(h->view(), k, da, db, static_cast<int16_t *>(dout), s);
+            PADO_CUDA(cudaMemcpyAsync(out, dout, k * osz, cudaMemcpyDeviceToHost, s));
+            PADO_CUDA(cudaFreeAsync(buf, s));
+            PADO_CUDA(cudaStreamSynchronize(s));
+        } catch (...) {
+            cudaFreeAsync(buf, s);
+            cudaStreamSynchronize(s);
+            throw;
+        }
+    });
+}
+
+int pado_store(const pado_index *h, const char *path)
+{
+    if (!h || !path) return fail(PADO_E_ARG, "null argument");
+    const uint32_t n = h->n, K = h->K;
+    const uint64_t tot = h->store.total;
+    std::vector<uint64_t> off(n + 1);
+    std::vector<uint32_t> hub(std::max<uint64_t>(tot, 1));
+    std::vector<uint8_t> dist(std::max<uint64_t>(tot, 1) * (h->kind == PADO_WEIGHTED ? 2 : 1));
+    std::vector<uint8_t> bpd((size_t)n * K);
+    std::vector<uint64_t> bps((size_t)n * K * 2);
+    int st = pado_export(h, off.data(), hub.data(), dist.data(), K ? bpd.data() : nullptr, K ? bps.data() : nullptr);
+    if (st != PADO_OK) return st;
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return fail(PADO_E_IO, std::string("cannot open ") + path);
+    f.write(reinterpret_cast<const char *>(&n), 4);
+    if (h->kind == PADO_UNWEIGHTED) f.write(reinterpret_cast<const char *>(&K), 4);
+    for (uint32_t v = 0; v < n; ++v) {
+        for (uint32_t i = 0; i < K; ++i) {
+            f.write(reinterpret_cast<const char *>(&bpd[(size_t)v * K + i]), 1);
+            f.write(reinterpret_cast<const char *>(&bps[((size_t)v * K + i) * 2]), 16);
+        }
+        const uint32_t cnt = (uint32_t)(off[v + 1] - off[v]);
+        f.write(reinterpret_cast<const char *>(&cnt), 4);
+        for (uint64_t j = off[v]; j < off[v + 1]; ++j) {
+            f.write(reinterpret_cast<const char *>(&hub[j]), 4);
+            if (h->kind == PADO_UNWEIGHTED)
+                f.write(reinterpret_cast<const char *>(&dist[j]), 1);
+            else
+                f.write(reinterpret_cast<const char *>(&dist[j * 2]), 2);
+        }
+    }
+    f.close();
+    if (!f) return fail(PADO_E_IO, std::string("write failed: ") + path);
+    return PADO_OK;
+}
+
+int pado_load(const char *path, uint32_t kind, pado_index **out)
+{
+    if (!path || !out) return fail(PADO_E_ARG, "null argument");
+    *out = nullptr;
+    if (kind != PADO_UNWEIGHTED && kind != PADO_WEIGHTED) return fail(PADO_E_ARG, "unknown index kind");
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(PADO_E_IO, std::string("cannot open ") + path);
+    uint32_t n = 0, K = 0;
+    auto rd = [&](void *p, size_t sz) { f.read(static_cast<char *>(p), sz); return (bool)f; };
+    if (!rd(&n, 4)) return fail(PADO_E_IO, "truncated index header");
+    if (kind == PADO_UNWEIGHTED && !rd(&K, 4)) return fail(PADO_E_IO, "truncated index header");
+    if (K > pado::MAX_BP) return fail(PADO_E_IO, "index has more than 64 bit-parallel roots");
+    std::vector<uint64_t> off(n + 1, 0);
+    std::vector<uint32_t> hub;
+    std::vector<uint8_t> d8;
+    std::vector<int16_t> d16;
+    std::vector<uint8_t> bpd((size_t)n * K);
+    std::vector<uint64_t> bps((size_t)n * K * 2);
+    for (uint32_t v = 0; v < n; ++v) {
+        for (uint32_t i = 0; i < K; ++i) {
+            if (!rd(&bpd[(size_t)v * K + i], 1) || !rd(&bps[((size_t)v * K + i) * 2], 16))
+                return fail(PADO_E_IO, "truncated bit-parallel rows");
+        }
+        uint32_t cnt = 0;
+        if (!rd(&cnt, 4)) return fail(PADO_E_IO, "truncated label count");
+        off[v + 1] = off[v] + cnt;
+        for (uint32_t j = 0; j < cnt; ++j) {
+            uint32_t x;
+            if (!rd(&x, 4)) return fail(PADO_E_IO, "truncated labels");
+            hub.push_back(x);
+            if (kind == PADO_UNWEIGHTED) {
+                uint8_t dd;
+                if (!rd(&dd, 1)) return fail(PADO_E_IO, "truncated labels");
+                d8.push_back(dd);
+            } else {
+                int16_t dd;
+                if (!rd(&dd, 2)) return fail(PADO_E_IO, "truncated labels");
+                d16.push_back(dd);
+            }
+        }
+    }
+    const void *dist = kind == PADO_UNWEIGHTED ? (const void *)d8.data() : (const void *)d16.data();
+    int st = pado_import(kind, n, K, off.data(), hub.data(), dist, K ? bpd.data() : nullptr, K ? bps.data() : nullptr, out);
+    if (st == PADO_E_ARG) return fail(PADO_E_IO, std::string("malformed index file: ") + g_err);
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,141 @@
+// pado_common.cuh -- shared device/host helpers for the PADO GPU library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "pado_gpu.h"
+
+namespace pado {
+
+constexpr uint8_t U8_INF = 255;      // includes/globals.h:37 (WEIGHTI_MAX)
+constexpr int16_t I16_INF = 32767;   // includes/globals.h:39 (WEIGHTILARGE_MAX)
+constexpr uint32_t MAX_BP = 64;      // bit-parallel roots the kernels support
+constexpr uint32_t MAX_BATCH = 2048; // root batch sizes the kernels support
+
+// Error carried from a failing CUDA call or argument check to the C ABI.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define PADO_CUDA(call)                                                                     \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            throw ::pado::Error(e_ == cudaErrorMemoryAllocation ? PADO_E_NOMEM : PADO_E_CUDA, \
+                                std::string(#call) + ": " + cudaGetErrorString(e_));       \
+    } while (0)
+
+#define PADO_CHECK(cond, code, msg)                                  \
+    do {                                                             \
+        if (!(cond)) throw ::pado::Error((code), (msg));             \
+    } while (0)
+
+// Owning device buffer.
+template <typename T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    explicit DBuf(size_t count) { alloc(count); }
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DBuf &operator=(DBuf &&o) noexcept
+    {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DBuf() { release(); }
+    void alloc(size_t count)
+    {
+        release();
+        if (count) PADO_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+        n = count;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+    void upload(const T *h, size_t count, cudaStream_t s = 0)
+    {
+        if (count) PADO_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void download(T *h, size_t count, cudaStream_t s = 0) const
+    {
+        if (count) PADO_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    }
+    void fill_bytes(int v, cudaStream_t s = 0)
+    {
+        if (n) PADO_CUDA(cudaMemsetAsync(p, v, bytes(), s));
+    }
+};
+
+inline unsigned grid_for(uint64_t items, unsigned block, unsigned cap = 152u * 64u)
+{
+    uint64_t g = (items + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+// Device-side status word bits (written by kernels, read by the host).
+enum : uint32_t {
+    ST_LEVEL_OVERFLOW = 1u,   // a BFS level reached 255 (uint8 distance)
+    ST_POOL_RETRY = 2u,       // a warp could not allocate label space
+    ST_BAD_INPUT = 4u,
+};
+
+// Launch accounting (profile.cu).  PADO_LAUNCH(name, stream, kernel<<<...>>>(...))
+// counts the launch, checks it, and times it while profiling is enabled.
+void check_launch(const char *what);
+bool profiling();
+void prof_begin(cudaStream_t s);
+void prof_end(const char *name, cudaStream_t s);
+#define PADO_LAUNCH(name, stream, ...)         \
+    do {                                       \
+        ::pado::prof_begin(stream);            \
+        __VA_ARGS__;                           \
+        ::pado::check_launch(name);            \
+        ::pado::prof_end(name, stream);        \
+    } while (0)
+
+// Device counters of algorithmic bytes, one slot per hot kernel (null unless
+// profiling).
+enum WorkSlot : int {
+    W_PULL = 0, W_MARK, W_BP_SIB, W_BP_CHILD, W_Q_UNW, W_Q_W, W_WPULL, W_WMARK, W_FINAL, WORK_SLOTS
+};
+const char *work_slot_name(int i);
+unsigned long long *work_counters();
+
+// Initial label-pool / round-log capacities (entries).  Both grow on demand;
+// PADO_DEBUG_POOL_ENTRIES (tests only) starts them tiny so that the exact
+// re-run path after a failed reservation is exercised on small graphs.
+inline uint64_t debug_pool_entries()
+{
+    const char *e = std::getenv("PADO_DEBUG_POOL_ENTRIES");
+    return e ? std::strtoull(e, nullptr, 10) : 0;
+}
+inline uint64_t initial_pool_entries(uint32_t n)
+{
+    const uint64_t dbg = debug_pool_entries();
+    return dbg ? dbg : std::max<uint64_t>((uint64_t)n * 16, 1u << 20);
+}
+inline uint64_t initial_log_entries(uint32_t n, uint32_t B)
+{
+    const uint64_t dbg = debug_pool_entries();
+    return dbg ? std::max<uint64_t>(dbg, B) : std::max<uint64_t>((uint64_t)n * 4, (uint64_t)B + (1u << 16));
+}
+
+}  // namespace pado

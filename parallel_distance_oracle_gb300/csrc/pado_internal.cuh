@@ -1,0 +1,81 @@
+// pado_internal.cuh -- device views and host launchers shared by the .cu files.
+#pragma once
+
+#include "pado_common.cuh"
+
+namespace pado {
+
+// Read-only view of a finished label set, indexed by RANK.  Queries map their
+// original-id endpoints through `rank` (identity when null).
+struct IndexView {
+    uint32_t n = 0;
+    uint32_t K = 0;             // bit-parallel roots (unweighted only)
+    const uint32_t *rank = nullptr;
+    const uint64_t *off = nullptr;   // n + 1
+    const uint32_t *hub = nullptr;   // rank-id hubs, ascending per vertex
+    const uint8_t *dist8 = nullptr;  // unweighted distances
+    const int16_t *dist16 = nullptr; // weighted distances
+    const uint8_t *bpd = nullptr;    // n * K
+    const uint64_t *bps = nullptr;   // n * K * 2  (S^-1, S^0)
+    unsigned long long *work = nullptr;  // profiling counters
+};
+
+// query.cu
+void launch_query_unw(const IndexView &v, uint64_t k, const uint32_t *a, const uint32_t *b, uint8_t *out,
+                      cudaStream_t s);
+void launch_query_w(const IndexView &v, uint64_t k, const uint32_t *a, const uint32_t *b, int16_t *out,
+                    cudaStream_t s);
+
+// A graph already relabeled by rank, neighbour lists in descending id order
+// (Graph::id_transfer, graph.h:176-206), on the device.
+struct DevGraph {
+    uint32_t n = 0;
+    uint64_t m = 0;              // directed entries
+    DBuf<uint32_t> off;          // n + 1 (m must fit 32 bits)
+    DBuf<uint32_t> adj;          // m
+    DBuf<uint8_t> w;             // m (weighted only)
+};
+
+// Host-side relabel + sort (graph.h:176-206 semantics).
+struct HostGraph {
+    uint32_t n = 0;
+    std::vector<uint32_t> off;
+    std::vector<uint32_t> adj;
+    std::vector<uint8_t> w;
+};
+HostGraph relabel_host(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w,
+                       const uint32_t *rank);
+
+// bp.cu: bit-parallel labeling (pado_unw_unv_unp.h:268-384).  `used` (host,
+// n) is updated with the roots and their selected neighbours.  Writes
+// bpd[n*K], bps[n*K*2] on the device.
+struct BpResult {
+    float ms = 0.f;
+    uint32_t levels = 0;
+};
+BpResult bp_label(const HostGraph &hg, const DevGraph &g, uint32_t K, std::vector<uint8_t> &used,
+                  uint8_t *d_bpd, uint64_t *d_bps, cudaStream_t s);
+
+// Final label store produced by a labeler (rank-indexed, sorted by hub).
+struct LabelStore {
+    DBuf<uint64_t> off;
+    DBuf<uint32_t> hub;
+    DBuf<uint8_t> dist8;
+    DBuf<int16_t> dist16;
+    uint64_t total = 0;
+};
+
+struct LabelRun {
+    float ms = 0.f;          // device time of the batch labeling
+    uint32_t levels = 0;
+    uint32_t batches = 0;
+};
+
+// unw.cu: batched pruned BFS labeling (pado_unw_unv_unp.h:425-1118).
+LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<uint8_t> &used,
+                   const uint8_t *d_bpd, const uint64_t *d_bps, LabelStore &out, cudaStream_t s);
+
+// weighted.cu: batched pruned relaxation (pado_weighted_unv_unp.h:281-1526).
+LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s);
+
+}  // namespace pado

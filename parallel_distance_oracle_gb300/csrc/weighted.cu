@@ -1,0 +1,726 @@
+// weighted.cu -- batched pruned relaxation labeling for weighted graphs.
+//
+// Restates WeightedVertexCentricPLL (reference
+// includes/pado_weighted_unv_unp.h:281-1526; OpenMP variant
+// includes/pado_weighted_unv_para.h:305-1706).  Per batch of B consecutive
+// ranks [s, e) (every vertex is a root; there are no BP labels):
+//   initialize (:281-330): roots_labels_buffer[c][h] = d for each committed
+//     label (h, d) of root c, buffer[c][c] = 0; each root holds the temporary
+//     label (c, 0) and is active.
+//   rounds until nothing is active:
+//     send (:409-474): an active head h relaxes every root c it accepted in the
+//       previous round to each neighbour t > c (lists are descending; t <= s
+//       ends the scan): m = (int16)(d_h(c) + w(h, t)) is kept when
+//       m < dists_table[t][c] and m < this round's best for (t, c);
+//       dists_table[t][c] becomes the round minimum.
+//     check (:476-870, :1300-1345): candidate (t, c, m) is pruned when
+//       (1) some committed label (h, d) of t has buffer[c][h] finite and
+//           d + buffer[c][h] <= m, or
+//       (2) some temporary label r < c of t gives d_t(r) + T[c][r] <= m, where
+//           T is the temporary table of the vertex whose id is c's batch-local
+//           index (:585) -- a no-op after batch 0, since those vertices hold no
+//           temporary labels then.
+//       Pruned with a smaller covering value q lowers dists_table[t][c] to q.
+//       Otherwise t's temporary label for c becomes m and t is active.
+//   filter (:1052-1184): drop temporary (v, c) when a temporary r < c of v has
+//     d_v(r) <= d_v(c), d_c(r) <= d_v(c) and d_v(r) + d_c(r) <= d_v(c).
+//   update_index (:913-950): append the survivors (hub = c's rank, int16 d).
+// Device schedule: the reference runs these phases in queue order on one
+// thread; here each round is level-synchronous -- all candidates of a round
+// are checked against the temporary labels as they stood when the round
+// started, and the filter reads the pre-filter values.  The CPU restatement of
+// exactly this schedule (the oracle's snapshot mode) produced byte-identical
+// label sets to the reference on every graph it was compared on.
+//
+// Device mapping: as in the unweighted labeler -- a mark kernel stamps the
+// tails of the active heads, and a pull kernel runs a warp per tail that owns
+// the tail's rows of dists_table / temporary labels for the round: it min-
+// reduces the incoming relaxations per root in shared memory, runs checks (1)
+// and (2) lane-per-candidate, and commits.  The previous round's accepted
+// (root, distance) pairs of each vertex are read from a parity-double-
+// buffered log, so heads can be read while their owners accept new roots.
+// dists_table entries carry a batch stamp and never need resetting.
+
+#include <algorithm>
+#include <climits>
+
+#include "pado_internal.cuh"
+
+namespace pado {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int WPULL_WARPS = 4;
+constexpr int32_t RMIN_EMPTY = INT_MAX;
+
+struct WDev {
+    uint32_t n, B;
+    const uint32_t *off;
+    const uint32_t *adj;
+    const uint8_t *w;
+    uint32_t *pool_hub;
+    int16_t *pool_dist;
+    unsigned long long pool_cap;
+    unsigned long long *pool_top;
+    uint64_t *lab_off;
+    uint32_t *lab_len;
+    uint32_t *lab_cap;
+    int16_t *buf;        // [B][n]  roots' committed labels
+    int16_t *vd;         // [n][B]  temporary label distances
+    uint16_t *vq;        // [n][B]  temporary label roots, first-acceptance order
+    uint32_t *vq_len;    // n
+    uint32_t *dt;        // [n][B]  (batch+1) << 16 | uint16 distance
+    uint32_t *log[2];    // accepted (c << 16 | uint16 d) of each round, by parity
+    unsigned long long log_cap;
+    unsigned long long *log_top;  // [2]
+    uint64_t *last_pos[2];
+    uint32_t *last_cnt[2];
+    uint32_t *last_min[2];
+    uint32_t *act_stamp;
+    uint32_t *tail_stamp;
+    int16_t *snap;       // [B][B] rows of vertices < B at round start (batch 0)
+    uint32_t *status;
+    unsigned long long *work;
+};
+
+__device__ __forceinline__ int32_t dt_get(const WDev &d, uint32_t t, uint32_t c, uint32_t stamp)
+{
+    const uint32_t x = d.dt[(uint64_t)t * d.B + c];
+    return (x >> 16) == stamp ? (int32_t)(int16_t)(x & 0xffffu) : (int32_t)I16_INF;
+}
+
+__device__ __forceinline__ void dt_put(const WDev &d, uint32_t t, uint32_t c, uint32_t stamp, int32_t v)
+{
+    d.dt[(uint64_t)t * d.B + c] = (stamp << 16) | (uint32_t)(uint16_t)(int16_t)v;
+}
+
+__device__ __forceinline__ uint32_t warp_min_u32(uint32_t v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+
+__device__ __forceinline__ bool warp_reserve_w(const WDev &d, uint32_t v, uint32_t need, uint64_t &base, int lane)
+{
+    const uint32_t len = d.lab_len[v], cap = d.lab_cap[v];
+    base = d.lab_off[v];
+    if (need <= cap) return true;
+    uint32_t ncap = max(max(2u * cap, need), 8u);
+    ncap = (ncap + 7u) & ~7u;
+    unsigned long long pos = 0;
+    if (lane == 0) pos = atomicAdd(d.pool_top, (unsigned long long)ncap);
+    pos = __shfl_sync(FULL, pos, 0);
+    if (pos + ncap > d.pool_cap) return false;
+    for (uint32_t j = lane; j < len; j += 32) {
+        d.pool_hub[pos + j] = d.pool_hub[base + j];
+        d.pool_dist[pos + j] = d.pool_dist[base + j];
+    }
+    __syncwarp();
+    if (lane == 0) {
+        d.lab_off[v] = pos;
+        d.lab_cap[v] = ncap;
+    }
+    base = pos;
+    return true;
+}
+
+// initialize_tables (pado_weighted_unv_unp.h:281-330)
+__global__ void __launch_bounds__(256) w_root_init_kernel(WDev d, uint32_t s, uint32_t nroots, uint32_t lid0,
+                                                          uint32_t *front, uint32_t *front_cnt, uint32_t *news,
+                                                          uint32_t *news_cnt)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const int p = lid0 & 1;
+    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nroots; c += nw) {
+        const uint32_t r = s + c;
+        int16_t *row = d.buf + (uint64_t)c * d.n;
+        const uint64_t base = d.lab_off[r];
+        const uint32_t len = d.lab_len[r];
+        for (uint32_t j = lane; j < len; j += 32) row[d.pool_hub[base + j]] = d.pool_dist[base + j];
+        __syncwarp();
+        if (lane == 0) {
+            row[r] = 0;
+            d.vq[(uint64_t)r * d.B] = (uint16_t)c;
+            d.vq_len[r] = 1;
+            d.vd[(uint64_t)r * d.B + c] = 0;
+            const unsigned long long pos = atomicAdd(&d.log_top[p], 1ull);
+            d.log[p][pos] = (uint32_t)c << 16;
+            d.last_pos[p][r] = pos;
+            d.last_cnt[p][r] = 1;
+            d.last_min[p][r] = r;
+            d.act_stamp[r] = lid0;
+            front[atomicAdd(front_cnt, 1u)] = r;
+            news[atomicAdd(news_cnt, 1u)] = r;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) w_mark_kernel(WDev d, const uint32_t *front, const uint32_t *front_cnt,
+                                                     uint32_t lid_cur, uint32_t *tails, uint32_t *tails_cnt)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t cnt = *front_cnt;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const int pp = (lid_cur - 1) & 1;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw) {
+        const uint32_t h = front[q];
+        const uint32_t mn = d.last_min[pp][h];
+        const uint32_t e_end = d.off[h + 1];
+        for (uint32_t e0 = d.off[h]; e0 < e_end; e0 += 32) {
+            const uint32_t e = e0 + lane;
+            const bool in = e < e_end;
+            const uint32_t t = in ? d.adj[e] : 0u;
+            const bool ok = in && t > mn;
+            if (ok && d.tail_stamp[t] != lid_cur) {
+                if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) tails[atomicAdd(tails_cnt, 1u)] = t;
+            }
+            if (__ballot_sync(FULL, in && !ok)) break;
+        }
+    }
+}
+
+__global__ void w_snap_kernel(WDev d, uint32_t rows)
+{
+    const uint64_t tot = (uint64_t)rows * d.B;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tot; i += (uint64_t)gridDim.x * blockDim.x)
+        d.snap[i] = d.vd[i];
+}
+
+// Per-warp dynamic shared memory: rmin[B] int32, res[B] int32, touched[B] u16.
+__global__ void __launch_bounds__(WPULL_WARPS * 32) w_pull_kernel(WDev d, const uint32_t *tails, const uint32_t *tails_cnt,
+                                                                  uint32_t s, uint32_t b, uint32_t lid_cur,
+                                                                  uint32_t *front_next, uint32_t *front_next_cnt,
+                                                                  uint32_t *news, uint32_t *news_cnt, uint32_t *retry,
+                                                                  uint32_t *retry_cnt)
+{
+    extern __shared__ __align__(16) unsigned char wsm[];
+    __shared__ uint32_t s_cnt[WPULL_WARPS][2];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    const uint32_t B = d.B;
+    int32_t *rmin = reinterpret_cast<int32_t *>(wsm) + (size_t)w * B;
+    int32_t *res = reinterpret_cast<int32_t *>(wsm) + (size_t)WPULL_WARPS * B + (size_t)w * B;
+    uint16_t *touched = reinterpret_cast<uint16_t *>(reinterpret_cast<int32_t *>(wsm) + (size_t)2 * WPULL_WARPS * B) +
+                        (size_t)w * B;
+    const uint32_t cnt = *tails_cnt;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const int pp = (lid_cur - 1) & 1, cp = lid_cur & 1;
+    const uint32_t lid_prev = lid_cur - 1;
+    const uint32_t stamp = b + 1;
+    for (uint32_t c = lane; c < B; c += 32) rmin[c] = RMIN_EMPTY;
+    __syncwarp();
+    unsigned long long bytes = 0;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw) {
+        const uint32_t t = tails[q];
+        bytes += 8;
+        if (lane == 0) s_cnt[w][0] = 0;
+        __syncwarp();
+        // (a) round minimum of the relaxations arriving at t, per root
+        const uint32_t e_end = d.off[t + 1];
+        for (uint32_t e0 = d.off[t]; e0 < e_end; e0 += 32) {
+            const uint32_t e = e0 + lane;
+            const bool in = e < e_end;
+            const uint32_t h = in ? d.adj[e] : 0u;
+            const bool ge = in && h >= s;
+            const bool act = ge && d.act_stamp[h] == lid_prev;
+            const int32_t wt = act ? (int32_t)d.w[e] : 0;
+            uint32_t mask = __ballot_sync(FULL, act);
+            bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull +
+                     __popc(mask) * 13ull;
+            while (mask) {
+                const int src = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const uint32_t hh = __shfl_sync(FULL, h, src);
+                const int32_t ww = __shfl_sync(FULL, wt, src);
+                const uint64_t pos = d.last_pos[pp][hh];
+                const uint32_t c = d.last_cnt[pp][hh];
+                bytes += 4ull * c;
+                for (uint32_t j = lane; j < c; j += 32) {
+                    const uint32_t x = d.log[pp][pos + j];
+                    const uint32_t cr = x >> 16;
+                    if (s + cr < t) {
+                        const int32_t m = (int32_t)(int16_t)((int32_t)(int16_t)(x & 0xffffu) + ww);
+                        const int32_t old = atomicMin(&rmin[cr], m);
+                        if (old == RMIN_EMPTY) touched[atomicAdd(&s_cnt[w][0], 1u)] = (uint16_t)cr;
+                    }
+                }
+            }
+            if (__ballot_sync(FULL, in && !ge)) break;
+        }
+        __syncwarp();
+        const uint32_t ntouch = s_cnt[w][0];
+        if (ntouch == 0) continue;
+        // (b) candidates: round minimum below dists_table; checks (1) and (2)
+        const uint64_t cbase = d.lab_off[t];
+        const uint32_t clen = d.lab_len[t];
+        const uint32_t vql = d.vq_len[t];
+        uint32_t nacc = 0, nnew = 0, mnacc = 0xffffffffu;
+        for (uint32_t i0 = 0; i0 < ntouch; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            bool acc = false, isnew = false;
+            if (i < ntouch) {
+                const uint32_t c = touched[i];
+                const int32_t m = rmin[c];
+                int32_t r = INT_MAX;  // INT_MAX: not a candidate
+                if (m < dt_get(d, t, c, stamp)) {
+                    r = INT_MIN;  // accepted unless pruned below
+                    const uint32_t creal = s + c;
+                    const int16_t *brow = d.buf + (uint64_t)c * d.n;
+                    for (uint32_t j = 0; j < clen; ++j) {
+                        const uint32_t hh = d.pool_hub[cbase + j];
+                        const int16_t bb = brow[hh];
+                        if (creal <= hh || bb == I16_INF) continue;
+                        const int32_t val = (int16_t)(d.pool_dist[cbase + j] + bb);
+                        if (val <= m) { r = val; break; }
+                    }
+                    if (r == INT_MIN && b == 0) {
+                        const int16_t *crow = d.snap + (uint64_t)c * B;
+                        const uint16_t *tq = d.vq + (uint64_t)t * B;
+                        const int16_t *trow = d.vd + (uint64_t)t * B;
+                        for (uint32_t k = 0; k < vql; ++k) {
+                            const uint32_t rr = tq[k];
+                            if (creal <= s + rr) continue;
+                            const int16_t sc = crow[rr];
+                            if (sc == I16_INF) continue;
+                            const int32_t val = (int16_t)(trow[rr] + sc);
+                            if (val <= m) { r = val; break; }
+                        }
+                    }
+                    if (r == INT_MIN) {
+                        acc = true;
+                        isnew = d.vd[(uint64_t)t * B + c] == I16_INF;
+                        mnacc = min(mnacc, creal);
+                    }
+                }
+                res[i] = r;
+            }
+            nacc += __popc(__ballot_sync(FULL, acc));
+            nnew += __popc(__ballot_sync(FULL, isnew));
+        }
+        mnacc = warp_min_u32(mnacc);
+        // dists_table reads, committed-label scans (6 B each), accepted entries
+        bytes += 4ull * ntouch + 12 + 6ull * clen * ntouch + 8ull * nacc;
+        // (c) reserve the log slots for the accepted roots, then commit
+        unsigned long long lpos = 0;
+        if (nacc) {
+            if (lane == 0) lpos = atomicAdd(&d.log_top[cp], (unsigned long long)nacc);
+            lpos = __shfl_sync(FULL, lpos, 0);
+            if (lpos + nacc > d.log_cap) {
+                if (lane == 0) {
+                    atomicOr(d.status, ST_POOL_RETRY);
+                    retry[atomicAdd(retry_cnt, 1u)] = t;
+                }
+                for (uint32_t i = lane; i < ntouch; i += 32) rmin[touched[i]] = RMIN_EMPTY;
+                __syncwarp();
+                continue;
+            }
+        }
+        if (lane == 0) s_cnt[w][1] = 0;
+        __syncwarp();
+        uint32_t accb = 0, newb = 0;
+        for (uint32_t i0 = 0; i0 < ntouch; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            bool acc = false, isnew = false;
+            uint32_t c = 0;
+            int32_t m = 0;
+            if (i < ntouch) {
+                c = touched[i];
+                m = rmin[c];
+                const int32_t r = res[i];
+                if (r != INT_MAX) {
+                    dt_put(d, t, c, stamp, m);
+                    if (r == INT_MIN) {
+                        acc = true;
+                        isnew = d.vd[(uint64_t)t * B + c] == I16_INF;
+                    } else if (r < m) {
+                        dt_put(d, t, c, stamp, r);
+                    }
+                }
+            }
+            const uint32_t am = __ballot_sync(FULL, acc), nm = __ballot_sync(FULL, isnew);
+            const uint32_t below = (1u << lane) - 1u;
+            if (acc) {
+                d.log[cp][lpos + accb + __popc(am & below)] = (c << 16) | (uint32_t)(uint16_t)(int16_t)m;
+                d.vd[(uint64_t)t * B + c] = (int16_t)m;
+            }
+            if (isnew) d.vq[(uint64_t)t * B + vql + newb + __popc(nm & below)] = (uint16_t)c;
+            accb += __popc(am);
+            newb += __popc(nm);
+        }
+        for (uint32_t i = lane; i < ntouch; i += 32) rmin[touched[i]] = RMIN_EMPTY;
+        __syncwarp();
+        bytes += 4ull * ntouch;  // dists_table writes
+        if (lane == 0) {
+            if (nnew) {
+                d.vq_len[t] = vql + nnew;
+                if (vql == 0) news[atomicAdd(news_cnt, 1u)] = t;
+            }
+            if (nacc) {
+                d.last_pos[cp][t] = lpos;
+                d.last_cnt[cp][t] = nacc;
+                d.last_min[cp][t] = mnacc;
+                d.act_stamp[t] = lid_cur;
+                front_next[atomicAdd(front_next_cnt, 1u)] = t;
+            }
+        }
+        __syncwarp();
+    }
+    if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_WPULL], bytes);
+}
+
+// filter_out_labels (pado_weighted_unv_unp.h:1052-1184) on pre-filter values;
+// a filtered entry gets bit 15 of its vq slot set.
+__global__ void __launch_bounds__(256) w_filter_kernel(WDev d, const uint32_t *news, uint32_t nnews, uint32_t s)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t B = d.B;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nnews; q += nw) {
+        const uint32_t v = news[q];
+        const uint32_t L = d.vq_len[v];
+        uint16_t *vq = d.vq + (uint64_t)v * B;
+        const int16_t *row = d.vd + (uint64_t)v * B;
+        for (uint32_t i0 = 0; i0 < L; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            bool filt = false;
+            if (i < L) {
+                const uint32_t c = vq[i] & 0x7fffu;
+                const int32_t dvc = row[c];
+                const int16_t *crow = d.vd + (uint64_t)(s + c) * B;
+                for (uint32_t k = 0; k < L && !filt; ++k) {
+                    const uint32_t r = vq[k] & 0x7fffu;
+                    if (c <= r) continue;
+                    const int32_t dvr = row[r];
+                    if (dvr > dvc) continue;
+                    const int32_t dcr = crow[r];
+                    if (dcr > dvc) continue;
+                    if (dvr + dcr <= dvc) filt = true;
+                }
+            }
+            __syncwarp();
+            if (filt) vq[i] |= 0x8000u;
+            __syncwarp();
+        }
+    }
+}
+
+// reset_tables for the roots' buffer rows (pado_weighted_unv_unp.h:872-891).
+__global__ void __launch_bounds__(256) w_buf_reset_kernel(WDev d, uint32_t s, uint32_t nroots)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nroots; c += nw) {
+        const uint32_t r = s + c;
+        int16_t *row = d.buf + (uint64_t)c * d.n;
+        const uint64_t base = d.lab_off[r];
+        const uint32_t len = d.lab_len[r];
+        for (uint32_t j = lane; j < len; j += 32) row[d.pool_hub[base + j]] = I16_INF;
+        if (lane == 0) row[r] = I16_INF;
+    }
+}
+
+// update_index (pado_weighted_unv_unp.h:913-950): append the unfiltered
+// temporary labels in ascending root order, then clear the temporary rows.
+__global__ void __launch_bounds__(256) w_commit_kernel(WDev d, const uint32_t *news, uint32_t nnews, uint32_t s,
+                                                       uint32_t *retry, uint32_t *retry_cnt)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t B = d.B;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nnews; q += nw) {
+        const uint32_t v = news[q];
+        const uint32_t L = d.vq_len[v];
+        uint16_t *vq = d.vq + (uint64_t)v * B;
+        int16_t *row = d.vd + (uint64_t)v * B;
+        uint32_t keep = 0;
+        for (uint32_t i = lane; i < L; i += 32) keep += (vq[i] & 0x8000u) ? 0u : 1u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) keep += __shfl_xor_sync(FULL, keep, o);
+        const uint32_t len = d.lab_len[v];
+        uint64_t base;
+        if (keep && !warp_reserve_w(d, v, len + keep, base, lane)) {
+            if (lane == 0) {
+                atomicOr(d.status, ST_POOL_RETRY);
+                retry[atomicAdd(retry_cnt, 1u)] = v;
+            }
+            continue;
+        }
+        if (keep) {
+            for (uint32_t i0 = 0; i0 < L; i0 += 32) {
+                const uint32_t i = i0 + lane;
+                const bool mine = i < L && !(vq[i] & 0x8000u);
+                const uint32_t key = mine ? vq[i] : 0xffffffffu;
+                uint32_t rank = 0;
+                for (uint32_t o0 = 0; o0 < L; o0 += 32) {
+                    const uint32_t oj = o0 + lane;
+                    const uint32_t other = (oj < L && !(vq[oj] & 0x8000u)) ? (uint32_t)vq[oj] : 0xffffffffu;
+                    for (int k = 0; k < 32; ++k) rank += (__shfl_sync(FULL, other, k) < key) ? 1u : 0u;
+                }
+                if (mine) {
+                    d.pool_hub[base + len + rank] = s + key;
+                    d.pool_dist[base + len + rank] = row[key];
+                }
+            }
+        }
+        __syncwarp();
+        for (uint32_t i = lane; i < L; i += 32) row[vq[i] & 0x7fffu] = I16_INF;
+        __syncwarp();
+        if (lane == 0) {
+            d.lab_len[v] = len + keep;
+            d.vq_len[v] = 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) w_compact_kernel(WDev d, const uint64_t *fin_off, uint32_t *fin_hub,
+                                                        int16_t *fin_dist)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < d.n; v += nw) {
+        const uint64_t base = d.lab_off[v], fo = fin_off[v];
+        const uint32_t len = d.lab_len[v];
+        for (uint32_t j = lane; j < len; j += 32) {
+            fin_hub[fo + j] = d.pool_hub[base + j];
+            fin_dist[fo + j] = d.pool_dist[base + j];
+        }
+    }
+}
+
+}  // namespace
+
+LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
+{
+    LabelRun run;
+    const uint32_t n = g.n;
+    PADO_CHECK(B >= 1 && B <= MAX_BATCH, PADO_E_ARG, "batch size must be in [1, 2048]");
+    PADO_CHECK(n < (1u << 31), PADO_E_ARG, "too many vertices");
+
+    uint64_t cap = initial_pool_entries(n);
+    uint64_t lcap = initial_log_entries(n, B);
+    DBuf<uint32_t> pool_hub(cap);
+    DBuf<int16_t> pool_dist(cap);
+    DBuf<unsigned long long> pool_top(1), log_top(2);
+    DBuf<uint64_t> lab_off(n), last_pos0(n), last_pos1(n);
+    DBuf<uint32_t> lab_len(n), lab_cap(n), last_cnt0(n), last_cnt1(n), last_min0(n), last_min1(n);
+    DBuf<uint32_t> act_stamp(n), tail_stamp(n), vq_len(n);
+    DBuf<int16_t> buf((uint64_t)B * n), vd((uint64_t)n * B), snap((uint64_t)B * B);
+    DBuf<uint16_t> vq((uint64_t)n * B);
+    DBuf<uint32_t> dt((uint64_t)n * B);
+    DBuf<uint32_t> log0(lcap), log1(lcap);
+    DBuf<uint32_t> front0(n), front1(n), tails(n), retry(n), news(n), counters(8), status(1);
+    pool_top.fill_bytes(0, s);
+    log_top.fill_bytes(0, s);
+    lab_off.fill_bytes(0, s);
+    lab_len.fill_bytes(0, s);
+    lab_cap.fill_bytes(0, s);
+    act_stamp.fill_bytes(0, s);
+    tail_stamp.fill_bytes(0, s);
+    vq_len.fill_bytes(0, s);
+    dt.fill_bytes(0, s);       // stamp 0 never matches a batch (stamps start at 1)
+    buf.fill_bytes(0xff, s);   // 0xffff is not INF: fixed just below
+    vd.fill_bytes(0xff, s);
+    status.fill_bytes(0, s);
+    {
+        // INF = 0x7fff for the int16 tables
+        auto fill_inf = [&](int16_t *p, uint64_t cnt) {
+            std::vector<int16_t> h(std::min<uint64_t>(cnt, 1u << 20), I16_INF);
+            for (uint64_t o = 0; o < cnt; o += h.size()) {
+                uint64_t k = std::min<uint64_t>(h.size(), cnt - o);
+                PADO_CUDA(cudaMemcpyAsync(p + o, h.data(), k * 2, cudaMemcpyHostToDevice, s));
+                PADO_CUDA(cudaStreamSynchronize(s));
+            }
+        };
+        fill_inf(buf.p, buf.n);
+        fill_inf(vd.p, vd.n);
+    }
+
+    WDev d{};
+    d.n = n;
+    d.B = B;
+    d.off = g.off.p;
+    d.adj = g.adj.p;
+    d.w = g.w.p;
+    d.pool_hub = pool_hub.p;
+    d.pool_dist = pool_dist.p;
+    d.pool_cap = cap;
+    d.pool_top = pool_top.p;
+    d.lab_off = lab_off.p;
+    d.lab_len = lab_len.p;
+    d.lab_cap = lab_cap.p;
+    d.buf = buf.p;
+    d.vd = vd.p;
+    d.vq = vq.p;
+    d.vq_len = vq_len.p;
+    d.dt = dt.p;
+    d.log[0] = log0.p;
+    d.log[1] = log1.p;
+    d.log_cap = lcap;
+    d.log_top = log_top.p;
+    d.last_pos[0] = last_pos0.p;
+    d.last_pos[1] = last_pos1.p;
+    d.last_cnt[0] = last_cnt0.p;
+    d.last_cnt[1] = last_cnt1.p;
+    d.last_min[0] = last_min0.p;
+    d.last_min[1] = last_min1.p;
+    d.act_stamp = act_stamp.p;
+    d.tail_stamp = tail_stamp.p;
+    d.snap = snap.p;
+    d.status = status.p;
+    d.work = work_counters();
+
+    const size_t pull_smem = (size_t)WPULL_WARPS * B * (4 + 4 + 2);
+    PADO_CUDA(cudaFuncSetAttribute(w_pull_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pull_smem));
+
+    struct Ctr { uint32_t front_next, tails, retry, news; unsigned long long top; unsigned long long ltop[2]; };
+    Ctr *hc = nullptr;
+    PADO_CUDA(cudaMallocHost((void **)&hc, sizeof(Ctr)));
+    uint32_t *c_front[2] = {counters.p + 0, counters.p + 1};
+    uint32_t *c_tails = counters.p + 2, *c_retry = counters.p + 3, *c_news = counters.p + 4;
+    uint32_t *fronts[2] = {front0.p, front1.p};
+    auto read_ctrs = [&](uint32_t *c_fn) {
+        PADO_CUDA(cudaMemcpyAsync(&hc->front_next, c_fn, 4, cudaMemcpyDeviceToHost, s));
+        PADO_CUDA(cudaMemcpyAsync(&hc->tails, c_tails, 4, cudaMemcpyDeviceToHost, s));
+        PADO_CUDA(cudaMemcpyAsync(&hc->retry, c_retry, 4, cudaMemcpyDeviceToHost, s));
+        PADO_CUDA(cudaMemcpyAsync(&hc->news, c_news, 4, cudaMemcpyDeviceToHost, s));
+        PADO_CUDA(cudaMemcpyAsync(&hc->top, pool_top.p, 8, cudaMemcpyDeviceToHost, s));
+        PADO_CUDA(cudaMemcpyAsync(&hc->ltop[0], log_top.p, 16, cudaMemcpyDeviceToHost, s));
+        PADO_CUDA(cudaStreamSynchronize(s));
+    };
+    auto grow_pool = [&](unsigned long long need) {
+        uint64_t ncap = std::max<uint64_t>(cap * 2, need + need / 2 + (1u << 20));
+        DBuf<uint32_t> nh(ncap);
+        DBuf<int16_t> nd(ncap);
+        PADO_CUDA(cudaMemcpyAsync(nh.p, pool_hub.p, cap * 4, cudaMemcpyDeviceToDevice, s));
+        PADO_CUDA(cudaMemcpyAsync(nd.p, pool_dist.p, cap * 2, cudaMemcpyDeviceToDevice, s));
+        PADO_CUDA(cudaStreamSynchronize(s));
+        pool_hub = std::move(nh);
+        pool_dist = std::move(nd);
+        cap = ncap;
+        d.pool_hub = pool_hub.p;
+        d.pool_dist = pool_dist.p;
+        d.pool_cap = cap;
+    };
+    // Grow both round logs (the one being written and the one being read).
+    auto grow_logs = [&](unsigned long long need) {
+        uint64_t ncap = std::max<uint64_t>(lcap * 2, need + need / 2);
+        DBuf<uint32_t> n0(ncap), n1(ncap);
+        PADO_CUDA(cudaMemcpyAsync(n0.p, log0.p, lcap * 4, cudaMemcpyDeviceToDevice, s));
+        PADO_CUDA(cudaMemcpyAsync(n1.p, log1.p, lcap * 4, cudaMemcpyDeviceToDevice, s));
+        PADO_CUDA(cudaStreamSynchronize(s));
+        log0 = std::move(n0);
+        log1 = std::move(n1);
+        lcap = ncap;
+        d.log[0] = log0.p;
+        d.log[1] = log1.p;
+        d.log_cap = lcap;
+    };
+
+    cudaEvent_t e0, e1;
+    PADO_CUDA(cudaEventCreate(&e0));
+    PADO_CUDA(cudaEventCreate(&e1));
+    PADO_CUDA(cudaEventRecord(e0, s));
+    uint32_t lid = 0;
+    try {
+        for (uint32_t bs = 0, b = 0; bs < n; bs += B, ++b) {
+            PADO_CHECK(b + 1 < 65536u, PADO_E_ARG, "more than 65534 batches");
+            const uint32_t nr = (uint32_t)std::min<uint64_t>(B, (uint64_t)n - bs);
+            ++run.batches;
+            const uint32_t lid0 = ++lid;
+            int cur = lid0 & 1;
+            PADO_CUDA(cudaMemsetAsync(counters.p, 0, 8 * sizeof(uint32_t), s));
+            PADO_CUDA(cudaMemsetAsync(&log_top.p[lid0 & 1], 0, 8, s));
+            PADO_LAUNCH("w_root_init_kernel", s,
+                        w_root_init_kernel<<<grid_for((uint64_t)nr * 32, 256), 256, 0, s>>>(d, bs, nr, lid0, fronts[cur], c_front[cur],
+                                                                                news.p, c_news));
+            uint32_t fsize = nr;
+            for (uint64_t round = 0; fsize > 0; ++round) {
+                // Bellman-Ford rounds are bounded by the vertex count
+                PADO_CHECK(round <= (uint64_t)n + 2, PADO_E_STATE, "relaxation did not converge");
+                const uint32_t lid_cur = ++lid;
+                const int nxt = cur ^ 1;
+                PADO_CUDA(cudaMemsetAsync(c_tails, 0, 4, s));
+                PADO_CUDA(cudaMemsetAsync(c_front[nxt], 0, 4, s));
+                PADO_CUDA(cudaMemsetAsync(&log_top.p[lid_cur & 1], 0, 8, s));
+                if (b == 0) {
+                    PADO_LAUNCH("w_snap_kernel", s,
+                                w_snap_kernel<<<grid_for((uint64_t)nr * B, 256), 256, 0, s>>>(d, nr));
+                }
+                PADO_LAUNCH("w_mark_kernel", s,
+                            w_mark_kernel<<<grid_for((uint64_t)fsize * 32, 256), 256, 0, s>>>(d, fronts[cur], c_front[cur], lid_cur,
+                                                                                 tails.p, c_tails));
+                PADO_LAUNCH("w_pull_kernel", s,
+                            w_pull_kernel<<<grid_for((uint64_t)n * 32, WPULL_WARPS * 32, 152u * 8u), WPULL_WARPS * 32, pull_smem, s>>>(
+                    d, tails.p, c_tails, bs, b, lid_cur, fronts[nxt], c_front[nxt], news.p, c_news, retry.p, c_retry));
+                read_ctrs(c_front[nxt]);
+                ++run.levels;
+                for (int attempt = 0; hc->retry; ++attempt) {
+                    PADO_CHECK(attempt < 64, PADO_E_NOMEM, "round log could not be grown enough");
+                    grow_logs(hc->ltop[lid_cur & 1]);
+                    PADO_CUDA(cudaMemcpyAsync(tails.p, retry.p, hc->retry * 4, cudaMemcpyDeviceToDevice, s));
+                    PADO_CUDA(cudaMemcpyAsync(c_tails, c_retry, 4, cudaMemcpyDeviceToDevice, s));
+                    PADO_CUDA(cudaMemsetAsync(c_retry, 0, 4, s));
+                    PADO_CUDA(cudaMemsetAsync(status.p, 0, 4, s));
+                    PADO_LAUNCH("w_pull_kernel(retry)", s,
+                                w_pull_kernel<<<grid_for((uint64_t)hc->retry * 32, WPULL_WARPS * 32, 152u * 8u), WPULL_WARPS * 32,
+                                    pull_smem, s>>>(d, tails.p, c_tails, bs, b, lid_cur, fronts[nxt], c_front[nxt],
+                                                    news.p, c_news, retry.p, c_retry));
+                    read_ctrs(c_front[nxt]);
+                }
+                fsize = hc->front_next;
+                cur = nxt;
+            }
+            read_ctrs(c_front[cur]);
+            const uint32_t nn = hc->news;
+            PADO_LAUNCH("w_filter_kernel", s,
+                        w_filter_kernel<<<grid_for((uint64_t)nn * 32, 256), 256, 0, s>>>(d, news.p, nn, bs));
+            PADO_LAUNCH("w_buf_reset_kernel", s,
+                        w_buf_reset_kernel<<<grid_for((uint64_t)nr * 32, 256), 256, 0, s>>>(d, bs, nr));
+            const uint32_t *clist = news.p;
+            uint32_t cn = nn;
+            for (int attempt = 0;; ++attempt) {
+                PADO_CHECK(attempt < 64, PADO_E_NOMEM, "label pool could not be grown enough");
+                PADO_LAUNCH("w_commit_kernel", s,
+                            w_commit_kernel<<<grid_for((uint64_t)cn * 32, 256), 256, 0, s>>>(d, clist, cn, bs, retry.p, c_retry));
+                read_ctrs(c_front[cur]);
+                if (!hc->retry) break;
+                grow_pool(hc->top);
+                PADO_CUDA(cudaMemcpyAsync(tails.p, retry.p, hc->retry * 4, cudaMemcpyDeviceToDevice, s));
+                PADO_CUDA(cudaMemsetAsync(c_retry, 0, 4, s));
+                PADO_CUDA(cudaMemsetAsync(status.p, 0, 4, s));
+                clist = tails.p;
+                cn = hc->retry;
+            }
+        }
+        std::vector<uint32_t> lens(n);
+        lab_len.download(lens.data(), n, s);
+        PADO_CUDA(cudaStreamSynchronize(s));
+        std::vector<uint64_t> fo(n + 1, 0);
+        for (uint32_t v = 0; v < n; ++v) fo[v + 1] = fo[v] + lens[v];
+        out.total = fo[n];
+        out.off.alloc(n + 1);
+        out.off.upload(fo.data(), n + 1, s);
+        out.hub.alloc(std::max<uint64_t>(out.total, 1));
+        out.dist16.alloc(std::max<uint64_t>(out.total, 1));
+        if (n) {
+            PADO_LAUNCH("w_compact_kernel", s,
+                        w_compact_kernel<<<grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(d, out.off.p, out.hub.p, out.dist16.p));
+        }
+        PADO_CUDA(cudaEventRecord(e1, s));
+        PADO_CUDA(cudaEventSynchronize(e1));
+        PADO_CUDA(cudaEventElapsedTime(&run.ms, e0, e1));
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFreeHost(hc);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeHost(hc);
+    return run;
+}
+
+}  // namespace pado

@@ -1,0 +1,218 @@
+"""Host-side mirror of the reference's labeler classes over the C ABI.
+
+The reference (includes/pado_unw_unv_unp.h, pado_unw_unv_para.*.h,
+pado_weighted_unv_{unp,para}.h) exposes one class per variant; the constructor
+labels a rank-relabeled graph, ``order_labels`` / ``load_index_from_file``
+install original ids, and ``query_distance(a, b)`` answers a pair.  The same
+names, argument meanings and results are kept here; each class is backed by a
+device-resident index built by the CUDA library.  Batched calls
+(``query``) are added beside the per-pair one.
+
+Errors raise :class:`PadoError` instead of the reference's print-and-exit.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import PADO_UNWEIGHTED, PADO_WEIGHTED, PadoError, check, lib, ptr
+from .graphs import CSRGraph
+
+U8_INF = 255
+I16_INF = 32767
+
+
+@dataclass
+class CanonicalLabels:
+    """The reference's Index after order_labels, keyed by original id."""
+    n: int
+    K: int
+    off: np.ndarray
+    hub: np.ndarray
+    dist: np.ndarray
+    bpd: np.ndarray | None = None
+    bps: np.ndarray | None = None
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def _u64(a):
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+class _Index:
+    kind = PADO_UNWEIGHTED
+
+    def __init__(self, handle: C.c_void_p | None = None):
+        self._h = handle
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.pado_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _need(self):
+        if not self._h:
+            raise PadoError(7, "index not built or loaded")
+        return self._h
+
+    # -- info ----------------------------------------------------------------
+    def info(self) -> _lib.Info:
+        inf = _lib.Info()
+        check(lib.pado_get_info(self._need(), C.byref(inf)))
+        return inf
+
+    @property
+    def num_v(self) -> int:
+        return self.info().n
+
+    # -- order / persistence ---------------------------------------------------
+    def order_labels(self, rank2id=None, rank=None) -> None:
+        """order_labels(rank2id, rank) (pado_unw_unv_unp.h:1227): queries take
+        original ids from now on.  Only ``rank`` is needed."""
+        if rank is None:
+            if rank2id is None:
+                raise ValueError("rank or rank2id required")
+            r2i = _u32(rank2id)
+            rank = np.empty_like(r2i)
+            rank[r2i] = np.arange(len(r2i), dtype=np.uint32)
+        check(lib.pado_set_order(self._need(), ptr(_u32(rank))))
+
+    def store_index_to_file(self, filename: str, rank=None) -> None:
+        """store_index_to_file (pado_unw_unv_unp.h:1120): reference format."""
+        if rank is not None:
+            self.order_labels(rank=rank)
+        check(lib.pado_store(self._need(), str(filename).encode()))
+
+    def load_index_from_file(self, filename: str) -> None:
+        """load_index_from_file (pado_unw_unv_unp.h:1182)."""
+        self.close()
+        h = C.c_void_p()
+        check(lib.pado_load(str(filename).encode(), self.kind, C.byref(h)))
+        self._h = h
+
+    # -- queries -------------------------------------------------------------
+    def query(self, a, b) -> np.ndarray:
+        """Batched query_distance over host arrays."""
+        a = _u32(a)
+        b = _u32(b)
+        if a.shape != b.shape:
+            raise ValueError("a and b must have the same shape")
+        out = np.empty(a.shape, dtype=np.uint8 if self.kind == PADO_UNWEIGHTED else np.int16)
+        check(lib.pado_query(self._need(), a.size, ptr(a), ptr(b), ptr(out)))
+        return out
+
+    def query_distance(self, a: int, b: int) -> int:
+        return int(self.query(np.array([a]), np.array([b]))[0])
+
+    def query_device(self, a_ptr: int, b_ptr: int, out_ptr: int, k: int, stream: int = 0) -> None:
+        """Queries on device arrays (raw pointers), enqueued on ``stream``."""
+        check(lib.pado_query_device(self._need(), k, C.c_void_p(a_ptr), C.c_void_p(b_ptr), C.c_void_p(out_ptr),
+                                    C.c_void_p(stream)))
+
+    # -- export --------------------------------------------------------------
+    def export(self) -> CanonicalLabels:
+        inf = self.info()
+        n, K, tot = inf.n, inf.bp_roots, inf.num_labels
+        off = np.zeros(n + 1, np.uint64)
+        hub = np.zeros(max(tot, 1), np.uint32)
+        dist = np.zeros(max(tot, 1), np.uint8 if self.kind == PADO_UNWEIGHTED else np.int16)
+        bpd = np.zeros(max(n * K, 1), np.uint8) if K else None
+        bps = np.zeros(max(n * K * 2, 1), np.uint64) if K else None
+        check(lib.pado_export(self._need(), ptr(off), ptr(hub), ptr(dist), ptr(bpd), ptr(bps)))
+        return CanonicalLabels(n, K, off, hub[:tot], dist[:tot],
+                               None if bpd is None else bpd[: n * K], None if bps is None else bps[: n * K * 2])
+
+
+class VertexCentricPLL(_Index):
+    """Unweighted labeler (reference VertexCentricPLL<BATCH_SIZE>,
+    pado_unw_unv_unp.h:42-257).
+
+    ``VertexCentricPLL(G, rank, bp_roots=50, batch=1024)`` labels the CSR graph
+    ``G`` (original ids) under vertex order ``rank`` and installs original
+    ids for queries.  ``rank=None`` means ``G`` is already rank-relabeled (the
+    reference's own precondition); call ``order_labels`` afterwards to query by
+    original id."""
+    kind = PADO_UNWEIGHTED
+
+    def __init__(self, G: CSRGraph | None = None, rank=None, bp_roots: int = 50, batch: int = 1024):
+        super().__init__()
+        self.bp_roots = bp_roots
+        self.batch = batch
+        if G is None:
+            return
+        h = C.c_void_p()
+        off, adj = _u64(G.off), _u32(G.adj)
+        if rank is None:
+            check(lib.pado_unw_build_ranked(G.n, ptr(off), ptr(adj), bp_roots, batch, C.byref(h)))
+        else:
+            check(lib.pado_unw_build(G.n, ptr(off), ptr(adj), ptr(_u32(rank)), bp_roots, batch, C.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_labels(cls, labels: CanonicalLabels) -> "VertexCentricPLL":
+        """Query-only index from canonical arrays (e.g. the reference's labels)."""
+        obj = cls()
+        h = C.c_void_p()
+        K = labels.K
+        dist = np.ascontiguousarray(labels.dist, dtype=np.uint8)
+        check(lib.pado_import(PADO_UNWEIGHTED, labels.n, K, ptr(_u64(labels.off)), ptr(_u32(labels.hub)), ptr(dist),
+                              ptr(np.ascontiguousarray(labels.bpd, np.uint8)) if K else None,
+                              ptr(np.ascontiguousarray(labels.bps, np.uint64)) if K else None, C.byref(h)))
+        obj._h = h
+        return obj
+
+
+# The OpenMP class of the reference computes the same labels
+# (pado_unw_unv_para.201912311607.parallel_bp_labeling.h:42-304).
+ParaVertexCentricPLL = VertexCentricPLL
+
+
+class WeightedVertexCentricPLL(_Index):
+    """Weighted labeler (reference WeightedVertexCentricPLL<BATCH_SIZE>,
+    pado_weighted_unv_unp.h:48-236); distances are int16, 32767 = unreachable."""
+    kind = PADO_WEIGHTED
+
+    def __init__(self, G: CSRGraph | None = None, rank=None, batch: int = 512):
+        super().__init__()
+        self.batch = batch
+        if G is None:
+            return
+        if G.w is None:
+            raise ValueError("weighted labeling needs edge weights (G.w)")
+        h = C.c_void_p()
+        off, adj, w = _u64(G.off), _u32(G.adj), np.ascontiguousarray(G.w, np.uint8)
+        if rank is None:
+            check(lib.pado_w_build_ranked(G.n, ptr(off), ptr(adj), ptr(w), batch, C.byref(h)))
+        else:
+            check(lib.pado_w_build(G.n, ptr(off), ptr(adj), ptr(w), ptr(_u32(rank)), batch, C.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_labels(cls, labels: CanonicalLabels) -> "WeightedVertexCentricPLL":
+        obj = cls()
+        h = C.c_void_p()
+        dist = np.ascontiguousarray(labels.dist, dtype=np.int16)
+        check(lib.pado_import(PADO_WEIGHTED, labels.n, 0, ptr(_u64(labels.off)), ptr(_u32(labels.hub)), ptr(dist),
+                              None, None, C.byref(h)))
+        obj._h = h
+        return obj
+
+
+WeightedParaVertexCentricPLL = WeightedVertexCentricPLL
+
+
+def version() -> str:
+    return lib.pado_version().decode()
