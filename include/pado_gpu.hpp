@@ -1,0 +1,280 @@
+// pado_gpu.hpp -- drop-in C++ classes over the C ABI (pado_gpu.h).
+//
+// The reference's drivers (pado.cpp, query_distance.cpp) use the labeler
+// classes this way:
+//     Graph G(file); rank = G.make_rank(); G.id_transfer(rank);
+//     auto *p = new ParaVertexCentricPLL<1024>(G);      // labels everything
+//     p->store_index_to_file(out, rank);
+//   and
+//     auto *q = new VertexCentricPLL<1024>(); q->load_index_from_file(idx);
+//     q->query_distance(a, b);
+// (pado.cpp:188-291, query_distance.cpp:55-73 of the reference).  The
+// classes below keep those names, template parameters and member signatures
+// (includes/pado_unw_unv_unp.h:236-257, pado_unw_unv_para.*.h:283-304,
+// pado_weighted_unv_unp.h:215-236, pado_weighted_unv_para.h:268-292), so the
+// drivers compile unchanged when this header replaces the labeler headers;
+// the labeling and the queries run on the GPU.  Include the reference's
+// globals.h/graph.h before this file, or let it include pado_gpu_graph.hpp.
+//
+// Added beside the reference's API: the constructor taking the vertex order,
+// the bit-parallel root count and the batch size; batched queries.
+// Errors in the reference's own methods print and exit, as the reference
+// does (pado_unw_unv_unp.h:1126-1129); the added methods throw
+// std::runtime_error.
+#ifndef PADO_GPU_HPP_
+#define PADO_GPU_HPP_
+
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <algorithm>
+#include <bitset>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <unordered_map>
+#include <utility>
+
+#include "pado_gpu.h"
+#ifndef INCLUDES_GRAPH_H_
+#include "pado_gpu_graph.hpp"
+#endif
+
+// The reference's labeler headers export these names at global scope
+// (pado_unw_unv_unp.h:26-34) and its drivers rely on them, so the drop-in
+// header exports the same ones.
+using std::bitset;
+using std::fill;
+using std::map;
+using std::min;
+using std::ofstream;
+using std::pair;
+using std::stable_sort;
+using std::unordered_map;
+using std::vector;
+
+namespace PADO {
+
+namespace gpu_detail {
+
+inline void die(int st)
+{
+    fprintf(stderr, "Error: %s (%s)\n", pado_last_error(), pado_status_string(st));
+    exit(EXIT_FAILURE);
+}
+
+inline void throw_on(int st)
+{
+    if (st != PADO_OK) throw std::runtime_error(std::string(pado_last_error()));
+}
+
+// 64-bit offsets of a reference-layout graph (vertices[] + out_degrees[]).
+template <typename G>
+inline std::vector<uint64_t> offsets(const G &g, std::vector<uint32_t> &adj_copy, const uint32_t *&adj)
+{
+    std::vector<uint64_t> off(g.num_v + 1, 0);
+    bool contiguous = true;
+    for (idi v = 0; v < g.num_v; ++v) {
+        off[v + 1] = off[v] + g.out_degrees[v];
+        if (g.vertices[v] != off[v]) contiguous = false;
+    }
+    if (contiguous) {
+        adj = g.out_edges;
+    } else {
+        adj_copy.resize(off[g.num_v]);
+        for (idi v = 0; v < g.num_v; ++v)
+            for (idi e = 0; e < g.out_degrees[v]; ++e) adj_copy[off[v] + e] = g.out_edges[g.vertices[v] + e];
+        adj = adj_copy.data();
+    }
+    return off;
+}
+
+class Handle {
+public:
+    pado_index *h = nullptr;
+    Handle() = default;
+    Handle(const Handle &) = delete;
+    Handle &operator=(const Handle &) = delete;
+    ~Handle() { pado_free(h); }
+    void reset(pado_index *x)
+    {
+        pado_free(h);
+        h = x;
+    }
+};
+
+}  // namespace gpu_detail
+
+// Unweighted labeler; the sequential and OpenMP classes of the reference label
+// identically, so both names map here.
+template <inti BATCH_SIZE = 1024>
+class VertexCentricPLL {
+public:
+    // The reference's class constant (pado_unw_unv_unp.h:46).
+    static const inti BITPARALLEL_SIZE = 50;
+    // Public statistics pair the reference keeps and pado.cpp prints
+    // (pado_unw_unv_unp.h:237); the GPU queries do not fill it.
+    std::pair<uint64_t, uint64_t> length_larger_than_16 = std::make_pair(0, 0);
+
+    VertexCentricPLL() = default;
+    // Labels a rank-relabeled graph (after Graph::id_transfer), like the
+    // reference constructor.
+    explicit VertexCentricPLL(const Graph &G) { build_ranked(G, BITPARALLEL_SIZE); }
+    // Extended: the original-id graph, its vertex order (rank[v] = position),
+    // the BP root count (<= 64) and the batch size (<= 2048); queries then
+    // take original ids directly.
+    VertexCentricPLL(const Graph &G, const std::vector<idi> &rank, inti bp_roots, inti batch_size)
+    {
+        std::vector<uint32_t> adj_copy;
+        const uint32_t *adj = nullptr;
+        std::vector<uint64_t> off = gpu_detail::offsets(G, adj_copy, adj);
+        pado_index *h = nullptr;
+        gpu_detail::throw_on(pado_unw_build(G.num_v, off.data(), adj, rank.data(), bp_roots, batch_size, &h));
+        idx_.reset(h);
+    }
+
+    void store_index_to_file(const char *filename, const std::vector<idi> &rank)
+    {
+        int st = pado_set_order(idx_.h, rank.data());
+        if (st == PADO_OK) st = pado_store(idx_.h, filename);
+        if (st != PADO_OK) gpu_detail::die(st);
+    }
+    void load_index_from_file(const char *filename)
+    {
+        pado_index *h = nullptr;
+        const int st = pado_load(filename, PADO_UNWEIGHTED, &h);
+        if (st != PADO_OK) gpu_detail::die(st);
+        idx_.reset(h);
+    }
+    void order_labels(const std::vector<idi> & /*rank2id*/, const std::vector<idi> &rank)
+    {
+        const int st = pado_set_order(idx_.h, rank.data());
+        if (st != PADO_OK) gpu_detail::die(st);
+    }
+    void switch_labels_to_old_id(const std::vector<idi> &rank2id, const std::vector<idi> &rank)
+    {
+        order_labels(rank2id, rank);
+    }
+    weighti query_distance(idi a, idi b)
+    {
+        weighti d = WEIGHTI_MAX;
+        const int st = pado_query(idx_.h, 1, &a, &b, &d);
+        if (st != PADO_OK) gpu_detail::die(st);
+        return d;
+    }
+    // Batched: out[i] = query_distance(a[i], b[i]).
+    void query_distance(const idi *a, const idi *b, size_t k, weighti *out)
+    {
+        gpu_detail::throw_on(pado_query(idx_.h, k, a, b, out));
+    }
+    pado_index *handle() const { return idx_.h; }
+
+private:
+    void build_ranked(const Graph &G, inti bp_roots)
+    {
+        std::vector<uint32_t> adj_copy;
+        const uint32_t *adj = nullptr;
+        std::vector<uint64_t> off = gpu_detail::offsets(G, adj_copy, adj);
+        pado_index *h = nullptr;
+        const int st = pado_unw_build_ranked(G.num_v, off.data(), adj, bp_roots, BATCH_SIZE, &h);
+        if (st != PADO_OK) gpu_detail::die(st);
+        idx_.reset(h);
+    }
+    gpu_detail::Handle idx_;
+};
+
+template <inti BATCH_SIZE>
+const inti VertexCentricPLL<BATCH_SIZE>::BITPARALLEL_SIZE;
+
+template <inti BATCH_SIZE = 1024>
+using ParaVertexCentricPLL = VertexCentricPLL<BATCH_SIZE>;
+
+template <inti BATCH_SIZE = 512>
+class WeightedVertexCentricPLL {
+public:
+    WeightedVertexCentricPLL() = default;
+    explicit WeightedVertexCentricPLL(const WeightedGraph &G)
+    {
+        std::vector<uint32_t> adj_copy;
+        const uint32_t *adj = nullptr;
+        std::vector<uint64_t> off = gpu_detail::offsets(G, adj_copy, adj);
+        std::vector<uint8_t> w(off[G.num_v]);
+        for (idi v = 0; v < G.num_v; ++v)
+            for (idi e = 0; e < G.out_degrees[v]; ++e) w[off[v] + e] = G.out_weights[G.vertices[v] + e];
+        pado_index *h = nullptr;
+        const int st = pado_w_build_ranked(G.num_v, off.data(), adj, w.data(), BATCH_SIZE, &h);
+        if (st != PADO_OK) gpu_detail::die(st);
+        idx_.reset(h);
+    }
+    WeightedVertexCentricPLL(const WeightedGraph &G, const std::vector<idi> &rank, inti batch_size)
+    {
+        std::vector<uint32_t> adj_copy;
+        const uint32_t *adj = nullptr;
+        std::vector<uint64_t> off = gpu_detail::offsets(G, adj_copy, adj);
+        std::vector<uint8_t> w(off[G.num_v]);
+        for (idi v = 0; v < G.num_v; ++v)
+            for (idi e = 0; e < G.out_degrees[v]; ++e) w[off[v] + e] = G.out_weights[G.vertices[v] + e];
+        pado_index *h = nullptr;
+        gpu_detail::throw_on(pado_w_build(G.num_v, off.data(), adj, w.data(), rank.data(), batch_size, &h));
+        idx_.reset(h);
+    }
+    void store_index_to_file(const char *filename, const std::vector<idi> &rank)
+    {
+        int st = pado_set_order(idx_.h, rank.data());
+        if (st == PADO_OK) st = pado_store(idx_.h, filename);
+        if (st != PADO_OK) gpu_detail::die(st);
+    }
+    void load_index_from_file(const char *filename)
+    {
+        pado_index *h = nullptr;
+        const int st = pado_load(filename, PADO_WEIGHTED, &h);
+        if (st != PADO_OK) gpu_detail::die(st);
+        idx_.reset(h);
+    }
+    void order_labels(const std::vector<idi> & /*rank2id*/, const std::vector<idi> &rank)
+    {
+        const int st = pado_set_order(idx_.h, rank.data());
+        if (st != PADO_OK) gpu_detail::die(st);
+    }
+    void switch_labels_to_old_id(const std::vector<idi> &rank2id, const std::vector<idi> &rank)
+    {
+        order_labels(rank2id, rank);
+    }
+    weightiLarge query_distance(idi a, idi b)
+    {
+        weightiLarge d = WEIGHTILARGE_MAX;
+        const int st = pado_query(idx_.h, 1, &a, &b, &d);
+        if (st != PADO_OK) gpu_detail::die(st);
+        return d;
+    }
+    void query_distance(const idi *a, const idi *b, size_t k, weightiLarge *out)
+    {
+        gpu_detail::throw_on(pado_query(idx_.h, k, a, b, out));
+    }
+    pado_index *handle() const { return idx_.h; }
+
+private:
+    gpu_detail::Handle idx_;
+};
+
+template <inti BATCH_SIZE = 512>
+using WeightedParaVertexCentricPLL = WeightedVertexCentricPLL<BATCH_SIZE>;
+
+// The AVX-512 classes of the reference (pado_unw_vec_{unp,para}.h,
+// pado_weighted_vec_{unp,para}.h; pado.cpp's -v 1 modes) compute the same
+// labels as the scalar ones, so they map onto the same GPU labelers.
+template <inti BATCH_SIZE = 1024>
+using VertexCentricPLLVec = VertexCentricPLL<BATCH_SIZE>;
+template <inti BATCH_SIZE = 1024>
+using ParaVertexCentricPLLVec = VertexCentricPLL<BATCH_SIZE>;
+template <inti BATCH_SIZE = 512>
+using WeightedVertexCentricPLLVec = WeightedVertexCentricPLL<BATCH_SIZE>;
+template <inti BATCH_SIZE = 512>
+using WeightedParaVertexCentricPLLVec = WeightedVertexCentricPLL<BATCH_SIZE>;
+
+}  // namespace PADO
+
+#endif  // PADO_GPU_HPP_

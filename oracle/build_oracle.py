@@ -76,8 +76,14 @@ def _patch(text: str) -> str:
     return text
 
 
+REF_DRIVERS = ["pado.cpp", "query_distance.cpp"]
+
+
 def stage_reference() -> bool:
-    """Write the patched header copy into oracle/_ref/inc.  False if no tree."""
+    """Write the patched header copy into oracle/_ref/inc, and unmodified
+    copies of the reference's two drivers into oracle/_ref/drivers (the
+    drop-in test builds them against include/pado_gpu.hpp).  False if no
+    tree."""
     src = _reference_dir() / "includes"
     if not src.is_dir():
         return False
@@ -85,6 +91,13 @@ def stage_reference() -> bool:
     for name in REF_HEADERS:
         out = REF_INC / name
         text = _patch((src / name).read_text(errors="replace"))
+        if not out.exists() or out.read_text(errors="replace") != text:
+            out.write_text(text)
+    drv = REF_OUT / "drivers"
+    drv.mkdir(parents=True, exist_ok=True)
+    for name in REF_DRIVERS:
+        text = (_reference_dir() / name).read_text(errors="replace")
+        out = drv / name
         if not out.exists() or out.read_text(errors="replace") != text:
             out.write_text(text)
     return True

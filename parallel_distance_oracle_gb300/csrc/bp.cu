@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(256) bp_sibling_kernel(BpState st, const uint3
         if (lane == 0 && acc) st.s0[v] |= acc;
         // front entry, offsets, S^0 update; 4 B adjacency + 4 B level per edge;
         // 8 B S^-1 per same-level neighbour
-        bytes += 20 + 8ull * (st.off[v + 1] - st.off[v]);
+        if (lane == 0) bytes += 20 + 8ull * (st.off[v + 1] - st.off[v]);
         bytes += 8ull * same;
     }
     if (st.work && bytes) atomicAdd(&st.work[W_BP_SIB], bytes);

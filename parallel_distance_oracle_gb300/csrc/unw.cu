@@ -73,7 +73,7 @@ struct UnwDev {
     uint64_t *last_pos[2];
     uint32_t *last_cnt[2];
     uint32_t *last_min[2];
-    uint32_t *act_stamp;
+    uint32_t *act_stamp[2];  // by level parity: level id at which the vertex gained labels
     uint32_t *tail_stamp;
     uint32_t *ind;        // n * words
     uint32_t *ind_stamp;  // batch + 1 when the row is valid
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) root_init_kernel(UnwDev d, const uint32_t
             d.last_pos[p][r] = base + len;
             d.last_cnt[p][r] = 1;
             d.last_min[p][r] = r;
-            d.act_stamp[r] = lid0;
+            d.act_stamp[p][r] = lid0;
             d.ind_stamp[r] = b + 1;
             front[atomicAdd(front_cnt, 1u)] = r;
         }
@@ -192,12 +192,14 @@ __global__ void __launch_bounds__(256) mark_kernel(UnwDev d, const uint32_t *fro
             const uint32_t t = in ? d.adj[e] : 0u;
             const bool ok = in && t > mn;
             bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
+            bool appended = false;
             if (ok && !d.used[t] && d.tail_stamp[t] != lid_cur) {
                 if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) {
                     tails[atomicAdd(tails_cnt, 1u)] = t;
-                    bytes += 8;
+                    appended = true;
                 }
             }
+            bytes += __popc(__ballot_sync(FULL, appended)) * 8ull;
             if (__ballot_sync(FULL, in && !ok)) break;  // descending: the rest are smaller
         }
     }
@@ -267,7 +269,7 @@ __global__ void __launch_bounds__(PULL_WARPS * 32) pull_kernel(UnwDev d, const u
             const bool in = e < e_end;
             const uint32_t h = in ? d.adj[e] : 0u;
             const bool ge = in && h >= s;
-            const bool act = ge && d.act_stamp[h] == lid_prev;
+            const bool act = ge && d.act_stamp[pp][h] == lid_prev;
             uint32_t mask = __ballot_sync(FULL, act);
             bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull;
             while (mask) {
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(PULL_WARPS * 32) pull_kernel(UnwDev d, const u
                 d.last_pos[cp][t] = base + len;
                 d.last_cnt[cp][t] = nadd;
                 d.last_min[cp][t] = mn;
-                d.act_stamp[t] = lid_cur;
+                d.act_stamp[cp][t] = lid_cur;
                 front_next[atomicAdd(front_next_cnt, 1u)] = t;
             }
         }
@@ -464,7 +466,7 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     DBuf<unsigned long long> pool_top(1);
     DBuf<uint64_t> lab_off(n), last_pos0(n), last_pos1(n);
     DBuf<uint32_t> lab_len(n), lab_cap(n), last_cnt0(n), last_cnt1(n), last_min0(n), last_min1(n);
-    DBuf<uint32_t> act_stamp(n), tail_stamp(n), ind_stamp(n);
+    DBuf<uint32_t> act_stamp0(n), act_stamp1(n), tail_stamp(n), ind_stamp(n);
     DBuf<uint32_t> ind((uint64_t)n * words);
     DBuf<uint8_t> dm((uint64_t)B * n);
     DBuf<uint32_t> front0(n), front1(n), tails(n), retry(n), counters(8), status(1);
@@ -473,7 +475,8 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     lab_off.fill_bytes(0, s);
     lab_len.fill_bytes(0, s);
     lab_cap.fill_bytes(0, s);
-    act_stamp.fill_bytes(0, s);
+    act_stamp0.fill_bytes(0, s);
+    act_stamp1.fill_bytes(0, s);
     tail_stamp.fill_bytes(0, s);
     ind_stamp.fill_bytes(0, s);
     dm.fill_bytes(0xff, s);
@@ -503,7 +506,8 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     d.last_cnt[1] = last_cnt1.p;
     d.last_min[0] = last_min0.p;
     d.last_min[1] = last_min1.p;
-    d.act_stamp = act_stamp.p;
+    d.act_stamp[0] = act_stamp0.p;
+    d.act_stamp[1] = act_stamp1.p;
     d.tail_stamp = tail_stamp.p;
     d.ind = ind.p;
     d.ind_stamp = ind_stamp.p;

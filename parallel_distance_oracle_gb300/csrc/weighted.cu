@@ -76,7 +76,7 @@ struct WDev {
     uint64_t *last_pos[2];
     uint32_t *last_cnt[2];
     uint32_t *last_min[2];
-    uint32_t *act_stamp;
+    uint32_t *act_stamp[2];  // by round parity: round id at which the vertex accepted roots
     uint32_t *tail_stamp;
     int16_t *snap;       // [B][B] rows of vertices < B at round start (batch 0)
     uint32_t *status;
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256) w_root_init_kernel(WDev d, uint32_t s, ui
             d.last_pos[p][r] = pos;
             d.last_cnt[p][r] = 1;
             d.last_min[p][r] = r;
-            d.act_stamp[r] = lid0;
+            d.act_stamp[p][r] = lid0;
             front[atomicAdd(front_cnt, 1u)] = r;
             news[atomicAdd(news_cnt, 1u)] = r;
         }
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32) w_pull_kernel(WDev d, const 
             const bool in = e < e_end;
             const uint32_t h = in ? d.adj[e] : 0u;
             const bool ge = in && h >= s;
-            const bool act = ge && d.act_stamp[h] == lid_prev;
+            const bool act = ge && d.act_stamp[pp][h] == lid_prev;
             const int32_t wt = act ? (int32_t)d.w[e] : 0;
             uint32_t mask = __ballot_sync(FULL, act);
             bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull +
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32) w_pull_kernel(WDev d, const 
                 d.last_pos[cp][t] = lpos;
                 d.last_cnt[cp][t] = nacc;
                 d.last_min[cp][t] = mnacc;
-                d.act_stamp[t] = lid_cur;
+                d.act_stamp[cp][t] = lid_cur;
                 front_next[atomicAdd(front_next_cnt, 1u)] = t;
             }
         }
@@ -505,7 +505,7 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
     DBuf<unsigned long long> pool_top(1), log_top(2);
     DBuf<uint64_t> lab_off(n), last_pos0(n), last_pos1(n);
     DBuf<uint32_t> lab_len(n), lab_cap(n), last_cnt0(n), last_cnt1(n), last_min0(n), last_min1(n);
-    DBuf<uint32_t> act_stamp(n), tail_stamp(n), vq_len(n);
+    DBuf<uint32_t> act_stamp0(n), act_stamp1(n), tail_stamp(n), vq_len(n);
     DBuf<int16_t> buf((uint64_t)B * n), vd((uint64_t)n * B), snap((uint64_t)B * B);
     DBuf<uint16_t> vq((uint64_t)n * B);
     DBuf<uint32_t> dt((uint64_t)n * B);
@@ -516,7 +516,8 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
     lab_off.fill_bytes(0, s);
     lab_len.fill_bytes(0, s);
     lab_cap.fill_bytes(0, s);
-    act_stamp.fill_bytes(0, s);
+    act_stamp0.fill_bytes(0, s);
+    act_stamp1.fill_bytes(0, s);
     tail_stamp.fill_bytes(0, s);
     vq_len.fill_bytes(0, s);
     dt.fill_bytes(0, s);       // stamp 0 never matches a batch (stamps start at 1)
@@ -565,7 +566,8 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
     d.last_cnt[1] = last_cnt1.p;
     d.last_min[0] = last_min0.p;
     d.last_min[1] = last_min1.p;
-    d.act_stamp = act_stamp.p;
+    d.act_stamp[0] = act_stamp0.p;
+    d.act_stamp[1] = act_stamp1.p;
     d.tail_stamp = tail_stamp.p;
     d.snap = snap.p;
     d.status = status.p;
