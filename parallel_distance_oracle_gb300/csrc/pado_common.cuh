@@ -114,7 +114,9 @@ void prof_end(const char *name, cudaStream_t s);
 // Device counters of algorithmic bytes, one slot per hot kernel (null unless
 // profiling).
 enum WorkSlot : int {
-    W_PULL = 0, W_MARK, W_BP_SIB, W_BP_CHILD, W_Q_UNW, W_Q_W, W_WPULL, W_WMARK, W_FINAL, WORK_SLOTS
+    W_PULL = 0, W_MARK, W_BP_SIB, W_BP_CHILD, W_Q_UNW, W_Q_W, W_WPULL, W_WMARK, W_FINAL,
+    // pull_kernel phase cycles (light tails, summed over warps)
+    W_CYC_SCAN, W_CYC_BP, W_CYC_DIST, W_CYC_COMMIT, W_CYC_HEAVY, WORK_SLOTS
 };
 const char *work_slot_name(int i);
 unsigned long long *work_counters();

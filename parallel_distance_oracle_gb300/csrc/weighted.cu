@@ -189,7 +189,7 @@ __global__ void w_snap_kernel(WDev d, uint32_t rows)
 }
 
 // Per-warp dynamic shared memory: rmin[B] int32, res[B] int32, touched[B] u16.
-__global__ void __launch_bounds__(WPULL_WARPS * 32) w_pull_kernel(WDev d, const uint32_t *tails, const uint32_t *tails_cnt,
+__global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_pull_kernel(WDev d, const uint32_t *tails, const uint32_t *tails_cnt,
                                                                   uint32_t s, uint32_t b, uint32_t lid_cur,
                                                                   uint32_t *front_next, uint32_t *front_next_cnt,
                                                                   uint32_t *news, uint32_t *news_cnt, uint32_t *retry,
