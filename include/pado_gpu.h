@@ -171,6 +171,22 @@ int pado_store(const pado_index *h, const char *path);
 int pado_load(const char *path, uint32_t kind, pado_index **out);
 
 /* ---------------------------------------------------------------------------
+ * Queries without device allocation.  No counterpart in the reference (whose
+ * queries run on the CPU).  For callers that must not have a library allocate
+ * device memory -- latency-bound serving threads, where cudaMalloc/cudaFree can
+ * block on device-wide synchronisation, and processes whose GPU memory is owned
+ * by another allocator: the pairs and results are staged through a fixed
+ * 2.5 MiB area compiled into the library (present on every GPU that loads it),
+ * so at most PADO_NOALLOC_MAX_PAIRS pairs per call (more -> PADO_E_ARG).
+ * Same arguments and results as pado_query; synchronous.  The first call on a
+ * device looks the area's address up (do it before any stream capture).  All
+ * calls on a device share the area: calls that overlap on the GPU (e.g. from
+ * two host threads at once) race on it and must be serialised by the caller.
+ * ------------------------------------------------------------------------- */
+#define PADO_NOALLOC_MAX_PAIRS 262144u
+int pado_query_noalloc(pado_index *h, uint64_t k, const uint32_t *a, const uint32_t *b, void *out);
+
+/* ---------------------------------------------------------------------------
  * Accounting (no counterpart in the reference, which prints wall-clock
  * timers such as Total_labeling_time, pado_unw_unv_unp.h:1000-1116).
  * ------------------------------------------------------------------------- */

@@ -58,6 +58,7 @@ def _load() -> C.CDLL:
         "pado_query_device": (C.c_int, [vp, u64, vp, vp, vp, vp]),
         "pado_store": (C.c_int, [vp, C.c_char_p]),
         "pado_load": (C.c_int, [C.c_char_p, u32, P(vp)]),
+        "pado_query_noalloc": (C.c_int, [vp, u64, vp, vp, vp]),
         "pado_kernel_launches": (u64, []),
         "pado_profile": (C.c_int, [C.c_int]),
         "pado_profile_read": (C.c_size_t, [C.c_char_p, C.c_size_t, C.c_int]),
@@ -75,7 +76,8 @@ lib = _load()
 EXPORTED = [
     "pado_last_error", "pado_status_string", "pado_version", "pado_unw_build", "pado_unw_build_ranked",
     "pado_w_build", "pado_w_build_ranked", "pado_set_order", "pado_free", "pado_get_info", "pado_export",
-    "pado_import", "pado_query", "pado_query_device", "pado_store", "pado_load", "pado_kernel_launches",
+    "pado_import", "pado_query", "pado_query_device", "pado_query_noalloc", "pado_store", "pado_load",
+    "pado_kernel_launches",
     "pado_profile", "pado_profile_read",
 ]
 

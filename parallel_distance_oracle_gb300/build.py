@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libpado_gpu.so"
-SOURCES = ["capi.cu", "query.cu", "bp.cu", "unw.cu", "weighted.cu", "profile.cu"]
+SOURCES = ["capi.cu", "query.cu", "bp.cu", "unw.cu", "weighted.cu", "profile.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

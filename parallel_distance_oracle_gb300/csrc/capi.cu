@@ -174,6 +174,11 @@ int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t 
 
 namespace pado {
 
+int set_error(int code, const std::string &msg) { return fail(code, msg); }
+IndexView index_view(const pado_index *h) { return h->view(); }
+uint32_t index_kind(const pado_index *h) { return h->kind; }
+int index_device(const pado_index *h) { return h->device; }
+
 HostGraph relabel_host(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, const uint32_t *rank)
 {
     HostGraph g;

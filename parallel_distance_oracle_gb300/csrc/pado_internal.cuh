@@ -78,4 +78,11 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
 // weighted.cu: batched pruned relaxation (pado_weighted_unv_unp.h:281-1526).
 LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s);
 
+// capi.cu: the calling thread's last-error message, and read-only access to
+// an index handle, for entry points defined in other files.
+int set_error(int code, const std::string &msg);
+IndexView index_view(const pado_index *h);
+uint32_t index_kind(const pado_index *h);
+int index_device(const pado_index *h);
+
 }  // namespace pado
