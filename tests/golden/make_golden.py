@@ -138,5 +138,58 @@ def _symmetric_weights(g, seed, lo, hi):
     return wu[inv].astype(np.uint8)
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--digests" not in sys.argv:
     main()
+
+
+# ---------------------------------------------------------------------------
+# Full-size digests: the configs' own graphs are too large to store, so the
+# reference's canonical label set for each is reduced to a SHA-256 digest of
+# (off, hub, dist[, bp_dist, bp_sets]) in that order, little-endian, plus the
+# label count.  Run:  python tests/golden/make_golden.py --digests
+# ---------------------------------------------------------------------------
+DIGEST_CASES = {
+    # R-MAT s14 ef8, degree order, K=50, B=1024
+    "rmat14_k50_b1024": dict(kind="unw", scale=14, ef=8, seed=1, K=50, B=1024),
+    # R-MAT s20 ef16, degree order, K=64, B=1024
+    "rmat20_k64_b1024": dict(kind="unw", scale=20, ef=16, seed=2, K=64, B=1024),
+    # weighted R-MAT s18 ef8, weights U[1,100], degree order, B=512
+    "wrmat18_b512": dict(kind="w", scale=18, ef=8, seed=3, K=0, B=512),
+}
+
+
+def label_digest(kind, off, hub, dist, bpd=None, bps=None):
+    import hashlib
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(off, np.uint64).tobytes())
+    h.update(np.ascontiguousarray(hub, np.uint32).tobytes())
+    h.update(np.ascontiguousarray(dist, np.uint8 if kind == "unw" else np.int16).tobytes())
+    if bpd is not None and len(bpd):
+        h.update(np.ascontiguousarray(bpd, np.uint8).tobytes())
+        h.update(np.ascontiguousarray(bps, np.uint64).tobytes())
+    return h.hexdigest()
+
+
+def digests():
+    import json
+    import os as _os
+    out = {}
+    for name, c in DIGEST_CASES.items():
+        w = (1, 100) if c["kind"] == "w" else None
+        g = G.rmat(c["scale"], c["ef"], c["seed"], weights=w)
+        rank = G.degree_rank(g)
+        threads = _os.cpu_count() or 1
+        if c["kind"] == "unw":
+            lab = orc.ref_unw_label(g, rank, c["K"], c["B"], mode=1, threads=threads)
+            dg = label_digest("unw", lab.off, lab.hub, lab.dist, lab.bpd, lab.bps)
+        else:
+            lab = orc.ref_w_label(g, rank, c["B"], mode=1, threads=threads)
+            dg = label_digest("w", lab.off, lab.hub, lab.dist)
+        out[name] = dict(c, labels=int(len(lab.hub)), sha256=dg, reference_seconds=round(lab.seconds, 2),
+                         reference_threads=threads)
+        print(name, out[name], flush=True)
+    (HERE / "full_size_digests.json").write_text(json.dumps(out, indent=1) + "\n")
+
+
+if __name__ == "__main__" and "--digests" in __import__("sys").argv:
+    digests()

@@ -103,7 +103,7 @@ def test_weighted_vs_oracle(pado, case):
 
 
 def test_c1_config_parity_and_bfs(pado):
-    """configs[0]: R-MAT s14/ef8, degree order, K=50, B=1024; 100k queries."""
+    """R-MAT s14/ef8, degree order, K=50, B=1024; 100k queries."""
     g = G.rmat(14, 8, 1)
     rank = G.degree_rank(g)
     idx, lab = gpu_unw(pado, g, rank, 50, 1024)

@@ -56,7 +56,7 @@ def test_oracle_weighted_queries_equal_dijkstra(seed):
 
 
 def test_oracle_c1_config_against_bfs():
-    # configs[0]: R-MAT s14 / ef 8 / K=50 / B=1024, sampled against BFS
+    # R-MAT s14 / ef 8 / K=50 / B=1024, sampled against BFS
     g = G.rmat(14, 8, 1)
     lab = orc.unw_label(g, G.degree_rank(g), 50, 1024)
     a, b = G.random_pairs(g.n, 2000, 11)
