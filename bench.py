@@ -34,19 +34,32 @@ sys.path.insert(0, str(REPO))
 from parallel_distance_oracle_gb300 import graphs as G  # noqa: E402
 
 WORKLOADS = {
-    # configs[1]: unweighted social-like R-MAT, 64 BP roots, batch 1024, 10M queries
+    # unweighted social-like R-MAT s20/ef16, 64 BP roots, batch 1024, 10M queries
     "rmat20": dict(kind="unw", scale=20, ef=16, seed=2, K=64, B=1024, queries=10_000_000, qseed=12,
                    desc="R-MAT s20 ef16 (a,b,c=.57,.19,.19), dedup+symmetrised, degree order, K=64, B=1024"),
-    # configs[0]: the CPU-runnable case
+    # R-MAT s14/ef8, K=50: the case a CPU labels in under a second
     "rmat14": dict(kind="unw", scale=14, ef=8, seed=1, K=50, B=1024, queries=100_000, qseed=11,
                    desc="R-MAT s14 ef8, degree order, K=50, B=1024"),
     # a smaller case of the same kernels, sized for ncu captures (a few GB on the device)
     "rmat18": dict(kind="unw", scale=18, ef=16, seed=2, K=64, B=1024, queries=1_000_000, qseed=12,
                    desc="R-MAT s18 ef16, degree order, K=64, B=1024 (profiling case)"),
-    # configs[2]: weighted R-MAT, weights 1..100, batch 512
+    # weighted R-MAT s18/ef8, weights 1..100, batch 512
     "wrmat18": dict(kind="w", scale=18, ef=8, seed=3, K=0, B=512, queries=1_000_000, qseed=13,
                     desc="weighted R-MAT s18 ef8, weights U[1,100], degree order, B=512"),
 }
+# Many independent graphs labeled together: 512 graphs, n log-uniform in
+# [1,000, n_hi], half Erdos-Renyi (average degree 6), half 2D grids with 2%
+# random long-range edges, each degree-ordered, 64 BP roots.  The batch size
+# is tuned over {256, 512, 1024, 2048} on a size-stratified sample, then the
+# batched build is compared with labeling the graphs one at a time.
+MANY = dict(graphs=512, n_lo=1000, n_hi=20000, er_degree=6, grid_frac=0.02, K=64, seed=5,
+            candidates=(256, 512, 1024, 2048), tune_sample=64)
+# Serving: label sets of the R-MAT s20 graph and 64 of the many-graph
+# workload's graphs in HBM under a 40 GB admission budget; open-loop Poisson
+# arrivals; each request asks one label set (uniform) for k pairs, k
+# log-uniform in [1, 65536], endpoints Zipf(1.1) over degree rank.
+SERVE = dict(budget=40 << 30, graphs=64, kmax=65536, zipf=1.1, rates=(1e4, 3e4, 1e5, 3e5, 1e6, 1e7),
+             pairs_per_rate=40_000_000, max_batch_pairs=1 << 20, slots=4, seed=9)
 METRIC = "labels_per_s"
 UNIT = "labels/s"
 
@@ -194,12 +207,19 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + ["many", "serve"])
+    ap.add_argument("--many-graphs", type=int, default=MANY["graphs"])
+    ap.add_argument("--many-nmax", type=int, default=MANY["n_hi"])
+    ap.add_argument("--many-batch", type=int, default=0, help="skip tuning and use this batch size")
     ap.add_argument("--queries", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-batches", type=int, default=1, help="root batches in one CPU-baseline sample")
     ap.add_argument("--no-profile", action="store_true")
     args = ap.parse_args()
+    if args.workload == "many":
+        return run_many(args)
+    if args.workload == "serve":
+        return run_serve(args)
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         return run_reference(args, wl)
@@ -395,6 +415,221 @@ def main():
         print(json.dumps(out), flush=True)
     if pg:
         pg.destroy_process_group()
+
+
+def many_graphs(count, n_lo, n_hi, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), size=count)).astype(np.int64)
+    gs = []
+    for i, n in enumerate(ns):
+        if i % 2 == 0:
+            gs.append(G.erdos_renyi(int(n), MANY["er_degree"], seed * 100_000 + i))
+        else:
+            gs.append(G.grid_with_shortcuts(int(n), MANY["grid_frac"], seed * 100_000 + i))
+    return gs
+
+
+def run_many(args):
+    """Batched labeling of many graphs vs one graph at a time (same GPU, same
+    batch size, same labels).  value = labels/s of the batched build's device
+    time; e2e = the same through pado_unw_build_many, wall clock, from host
+    CSR arrays to device-resident indexes."""
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the many-graph workload has no reference arm; "
+                          "the reference labels one graph per process"}))
+        return
+    import torch
+    torch.cuda.set_device(0)
+    from parallel_distance_oracle_gb300 import _lib, pado
+    lib = _lib.lib
+    K = MANY["K"]
+    t = time.perf_counter()
+    gs = many_graphs(args.many_graphs, MANY["n_lo"], args.many_nmax, MANY["seed"])
+    ranks = [G.degree_rank(g) for g in gs]
+    n_tot = sum(g.n for g in gs)
+    log(f"{len(gs)} graphs, {n_tot} vertices, {sum(g.m_directed for g in gs)} directed edges "
+        f"({time.perf_counter() - t:.1f}s to generate)")
+    tune = None
+    if args.many_batch:
+        B = args.many_batch
+    else:
+        t = time.perf_counter()
+        B, tms = pado.tune_batch(gs, ranks, bp_roots=K, candidates=MANY["candidates"], sample=MANY["tune_sample"])
+        tune = {"candidates_ms": tms, "sample_graphs": MANY["tune_sample"], "best": B,
+                "wall_s": time.perf_counter() - t}
+        log(f"tuned batch size {B}: {tms}")
+
+    def batched():
+        t0 = time.perf_counter()
+        idxs = pado.build_many(gs, ranks, bp_roots=K, batch=B)
+        wall = time.perf_counter() - t0
+        inf = idxs[0].info()
+        counts = [ix.info().num_labels for ix in idxs]
+        return idxs, inf.build_seconds, inf.bp_seconds, wall, counts, inf.levels
+
+    for i in range(args.warmup):
+        idxs, dev, bp, wall, counts, levels = batched()
+        log(f"warmup {i}: batched device {dev:.3f}s wall {wall:.3f}s labels {sum(counts)}")
+        for ix in idxs:
+            ix.close()
+    torch.cuda.synchronize()
+    launches0 = lib.pado_kernel_launches()
+    dev_s, wall_s = [], []
+    with ClockSampler(0) as clk:
+        for i in range(args.steps):
+            idxs, dev, bp, wall, counts, levels = batched()
+            dev_s.append(dev)
+            wall_s.append(wall)
+            log(f"step {i}: batched device {dev:.4f}s (bp {bp:.4f}s) wall {wall:.3f}s steps {levels}")
+            for ix in idxs:
+                ix.close()
+    torch.cuda.synchronize()
+    launches = (lib.pado_kernel_launches() - launches0) // max(args.steps, 1)
+    clocks = clk.summary()
+    labels = sum(counts)
+
+    # one graph at a time: the plain drop-in build, graph after graph
+    l0 = lib.pado_kernel_launches()
+    t0 = time.perf_counter()
+    one_dev = 0.0
+    one_counts = []
+    for g, rk in zip(gs, ranks):
+        ix = pado.VertexCentricPLL(g, rk, bp_roots=K, batch=B)
+        inf = ix.info()
+        one_dev += inf.build_seconds
+        one_counts.append(inf.num_labels)
+        ix.close()
+    one_wall = time.perf_counter() - t0
+    one_launches = lib.pado_kernel_launches() - l0
+    assert one_counts == counts, "batched and one-at-a-time label counts differ"
+    dev_mean, wall_mean = statistics.mean(dev_s), statistics.mean(wall_s)
+    out = {
+        "metric": METRIC, "value": labels / dev_mean, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_mean * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "many", "graphs": len(gs), "n_range": [MANY["n_lo"], args.many_nmax],
+                   "n_total": n_tot, "mix": "half Erdos-Renyi avg degree 6, half grid + 2% long-range edges",
+                   "bp_roots": K, "batch": B, "l2": "inputs larger than L2 (graphs + label state)"},
+        "labels": labels, "batched": {"device_s": dev_mean, "wall_s": wall_mean, "steps": levels,
+                                      "gpu_launches_per_build": launches},
+        "one_at_a_time": {"device_s": one_dev, "wall_s": one_wall, "gpu_launches": one_launches},
+        "speedup_device": one_dev / dev_mean, "speedup_wall": one_wall / wall_mean,
+        "tune": tune,
+        "e2e": {"value": labels / wall_mean, "unit": UNIT,
+                "h2d_bytes_per_step": int(sum(g.off.nbytes + g.adj.nbytes for g in gs)),
+                "d2h_bytes_per_step": 0, "note": "host CSR arrays in, device-resident indexes out"},
+        "clocks": clocks, "gpu_launches": launches,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_serve(args):
+    """Continuous-batching serving loop vs one launch per request, swept over
+    arrival rates.  value = queries/s of the batched loop at the highest rate
+    whose p99 latency stays under 1 ms."""
+    if args.impl == "reference":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop; its "
+                          "query_distance answers one pair per call on the host"}))
+        return
+    import torch
+    torch.cuda.set_device(0)
+    from parallel_distance_oracle_gb300 import _lib, pado
+    lib = _lib.lib
+    rng = np.random.Generator(np.random.PCG64(SERVE["seed"]))
+    t = time.perf_counter()
+    big = G.rmat(20, 16, 2)
+    rk_big = G.degree_rank(big)
+    sets = [(big, rk_big, pado.VertexCentricPLL(big, rk_big, bp_roots=64, batch=1024))]
+    gs = many_graphs(SERVE["graphs"], MANY["n_lo"], MANY["n_hi"], MANY["seed"])
+    rks = [G.degree_rank(g) for g in gs]
+    for g, rk, ix in zip(gs, rks, pado.build_many(gs, rks, bp_roots=MANY["K"], batch=1024)):
+        sets.append((g, rk, ix))
+    resident = sum(ix.info().device_bytes for _, _, ix in sets)
+    log(f"{len(sets)} label sets, {resident / 1e9:.2f} GB ({time.perf_counter() - t:.1f}s to build)")
+    # endpoint pools: Zipf(1.1) over degree rank, per label set
+    pool_n = 1 << 20
+    pools = []
+    for g, rk, _ in sets:
+        order = np.argsort(rk).astype(np.uint32)
+        pools.append((order[np.minimum(rng.zipf(SERVE["zipf"], size=pool_n) - 1, g.n - 1)],
+                      order[np.minimum(rng.zipf(SERVE["zipf"], size=pool_n) - 1, g.n - 1)]))
+
+    def trace(rate):
+        mean_k = (SERVE["kmax"] - 1) / np.log(SERVE["kmax"])
+        nreq = int(max(500, min(40_000, SERVE["pairs_per_rate"] / mean_k)))
+        arrival = np.cumsum(rng.exponential(1.0 / rate, size=nreq))
+        ids = rng.integers(0, len(sets), size=nreq).astype(np.uint32)
+        ks = np.minimum(np.exp(rng.uniform(0, np.log(SERVE["kmax"] + 1), size=nreq)).astype(np.uint64),
+                        SERVE["kmax"])
+        ks = np.maximum(ks, 1)
+        starts = rng.integers(0, pool_n - SERVE["kmax"], size=nreq)
+        a = np.concatenate([pools[i][0][s:s + int(k)] for i, s, k in zip(ids, starts, ks)])
+        b = np.concatenate([pools[i][1][s:s + int(k)] for i, s, k in zip(ids, starts, ks)])
+        return arrival, ids, ks, a, b
+
+    srv = pado.Server(SERVE["budget"], max_batch_pairs=SERVE["max_batch_pairs"], slots=SERVE["slots"])
+    for _, _, ix in sets:
+        srv.add(ix)
+    # warm-up: one short trace through both paths
+    wa = trace(1e5)
+    for mode in (0, 1):
+        srv.replay(*[x[:200] for x in wa[:3]], wa[3][:int(wa[2][:200].sum())], wa[4][:int(wa[2][:200].sum())],
+                   mode=mode)
+    sweep = []
+    checks = []
+    launches0 = lib.pado_kernel_launches()
+    with ClockSampler(0) as clk:
+        for rate in SERVE["rates"]:
+            arrival, ids, ks, a, b = trace(rate)
+            row = {"rate_req_s": rate, "requests": int(len(ks)), "pairs": int(ks.sum())}
+            for mode, name in ((0, "batched"), (1, "unbatched")):
+                st0 = srv.stats()
+                out8, _, lat = srv.replay(arrival, ids, ks, a, b, mode=mode)
+                st1 = srv.stats()
+                end = float(np.max(arrival + lat))
+                row[name] = {"p50_ms": float(np.percentile(lat, 50) * 1e3),
+                             "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                             "queries_per_s": float(ks.sum() / end),
+                             "batches": int(st1["batches"] - st0["batches"])}
+                if mode == 0:
+                    checks.append((ids[:50].copy(), ks[:50].copy(), a[:int(ks[:50].sum())].copy(),
+                                   b[:int(ks[:50].sum())].copy(), out8[:int(ks[:50].sum())].copy()))
+            log(f"rate {rate:.0e}: {row}")
+            sweep.append(row)
+    launches = lib.pado_kernel_launches() - launches0
+    clocks = clk.summary()
+    stats = srv.stats()
+    srv.close()
+    # results of the first requests of every rate equal pado_query on the same pairs
+    for ids, ks, a, b, out in checks:
+        off = 0
+        for i, k in zip(ids, ks):
+            k = int(k)
+            assert np.array_equal(out[off:off + k], sets[i][2].query(a[off:off + k], b[off:off + k])), \
+                "serving result differs from pado_query"
+            off += k
+    ok = [r for r in sweep if r["batched"]["p99_ms"] < 1.0]
+    best = max(ok, key=lambda r: r["batched"]["queries_per_s"]) if ok else None
+    best_unb = [r for r in sweep if r["unbatched"]["p99_ms"] < 1.0]
+    best_unb = max(best_unb, key=lambda r: r["unbatched"]["queries_per_s"]) if best_unb else None
+    peak_b = max(sweep, key=lambda r: r["batched"]["queries_per_s"])
+    out = {
+        "metric": "queries_per_s_at_p99_under_1ms", "value": best["batched"]["queries_per_s"] if best else None,
+        "unit": "queries/s", "n_gpus": 1, "steps": len(sweep), "warmup": 1, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "serve", "label_sets": len(sets), "resident_gb": resident / 1e9,
+                   "budget_gb": SERVE["budget"] / 1e9, "k": f"log-uniform [1, {SERVE['kmax']}]",
+                   "endpoints": f"Zipf({SERVE['zipf']}) over degree rank", "arrivals": "Poisson, open loop",
+                   "max_batch_pairs": SERVE["max_batch_pairs"], "slots": SERVE["slots"]},
+        "best_rate": best["rate_req_s"] if best else None,
+        "unbatched_value": best_unb["unbatched"]["queries_per_s"] if best_unb else None,
+        "peak_batched_queries_per_s": peak_b["batched"]["queries_per_s"],
+        "sweep": sweep, "server_stats": stats, "clocks": clocks, "gpu_launches": launches,
+        "e2e": {"value": best["batched"]["queries_per_s"] if best else None, "unit": "queries/s",
+                "h2d_bytes_per_step": 8, "d2h_bytes_per_step": 1,
+                "note": "per pair, host arrays in and out through pado_server_replay"},
+    }
+    print(json.dumps(out), flush=True)
 
 
 def traffic_from_profiles(kernel: str, workload: str):

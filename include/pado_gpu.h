@@ -93,6 +93,31 @@ int pado_unw_build(uint32_t n, const uint64_t *off, const uint32_t *adj, const u
 int pado_unw_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, uint32_t bp_roots,
                           uint32_t batch, pado_index **out);
 
+/* Labels G independent unweighted graphs together and returns one index per
+ * graph in out[0..G): every graph gets exactly the labels pado_unw_build
+ * would give it alone (same bp_roots and batch), but one persistent launch
+ * advances all graphs by one BFS level per step, so small graphs no longer
+ * cost a launch sequence each.  Graph i has n[i] vertices, CSR off[i]
+ * (n[i] + 1 entries) and adj[i], and vertex order rank[i] (rank itself or
+ * rank[i] NULL: the ids are already ranks, as in pado_unw_build_ranked).
+ * Replaces calling the labeling constructor (pado_unw_unv_unp.h:176-189) once
+ * per graph.  Sum of n[i] < 2^32 - 1, 1 <= G <= 65535.  On error no handle is
+ * returned. */
+int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *off,
+                        const uint32_t *const *adj, const uint32_t *const *rank,
+                        uint32_t bp_roots, uint32_t batch, pado_index **out);
+
+/* Batch-size tuner for pado_unw_build_many: labels `sample` of the graphs
+ * (evenly spaced in size order, smallest and largest included; 0 = all) once
+ * per candidate batch size in candidates[0..ncand), times each on the device
+ * and writes the fastest to *best (ms[c], if not NULL, receives candidate c's
+ * time).  The labels depend on the batch size (as the reference's do), so
+ * the tuned size is an input the caller then passes to pado_unw_build_many. */
+int pado_unw_tune_batch(uint32_t G, const uint32_t *n, const uint64_t *const *off,
+                        const uint32_t *const *adj, const uint32_t *const *rank,
+                        uint32_t bp_roots, const uint32_t *candidates, uint32_t ncand,
+                        uint32_t sample, uint32_t *best, float *ms);
+
 /* Weighted labeling; replaces
  *   WeightedVertexCentricPLL<BATCH_SIZE>::WeightedVertexCentricPLL(const WeightedGraph &)
  *     (includes/pado_weighted_unv_unp.h:275-279, construct :1408-1526)
@@ -192,6 +217,56 @@ int pado_query_noalloc(pado_index *h, uint64_t k, const uint32_t *a, const uint3
  * ------------------------------------------------------------------------- */
 /* Kernel launches this library has made in the process so far. */
 uint64_t pado_kernel_launches(void);
+
+/* ---------------------------------------------------------------------------
+ * Serving loop (continuous batching).  The reference answers pairs one call
+ * at a time on the host (query_distance, pado_unw_unv_unp.h:1312-1445, driven
+ * by query_distance.cpp:25-78); a server keeps label sets in HBM and
+ * coalesces concurrently arriving requests of any size into mixed batches:
+ * up to `slots` batches of at most max_batch_pairs pairs are in flight, each
+ * answered by one kernel launch, and requests that arrive meanwhile fill the
+ * next free slot.  Label sets are admitted and evicted (offloaded to
+ * page-locked host memory, least recently used first) to keep the resident
+ * bytes within hbm_budget_bytes and free HBM.  A request's results are the
+ * same as pado_query's on its own, whatever else is in the batch.
+ * ------------------------------------------------------------------------- */
+typedef struct pado_server pado_server;
+
+typedef struct pado_server_stats {
+    uint64_t requests, batches, pairs, max_batch_pairs;
+    uint64_t admissions, evictions;   /* label sets copied in / offloaded */
+    uint64_t resident_bytes;
+    uint32_t resident_indexes, pad;
+} pado_server_stats;
+
+int pado_server_create(uint64_t hbm_budget_bytes, uint32_t max_batch_pairs, uint32_t slots,
+                       pado_server **out);
+/* Registers an index (built or loaded, on the server's device).  The server
+ * borrows the handle: it may offload and reload its device arrays, and the
+ * caller must not use or free the handle until pado_server_destroy, which
+ * leaves every registered handle resident again. */
+int pado_server_add(pado_server *s, pado_index *h, uint32_t *index_id);
+/* Queues k pairs for index index_id; a, b and out (uint8 unweighted, int16
+ * weighted) must stay valid until the request completes.  Every ticket must
+ * be waited for once. */
+int pado_server_submit(pado_server *s, uint32_t index_id, uint64_t k, const uint32_t *a,
+                       const uint32_t *b, void *out, uint64_t *ticket);
+/* Waits (timeout_s < 0: forever) and reports the request's latency from
+ * submission to completion. */
+int pado_server_wait(pado_server *s, uint64_t ticket, double timeout_s, double *latency_s);
+int pado_server_get_stats(pado_server *s, pado_server_stats *out);
+/* Open-loop load replay: request i arrives arrival_s[i] seconds after the
+ * start (non-decreasing), asks index_id[i] for the k[i] pairs at
+ * a/b[pair_off[i] ...], and writes its results to out8 (unweighted) or out16
+ * (weighted) at pair_off[i].  mode 0 submits through the serving loop; mode 1
+ * answers each request on its own (copy in, one launch, copy back, in arrival
+ * order) as the unbatched comparison.  latency_s[i] = completion time minus
+ * scheduled arrival, so queueing behind a slow generator counts. */
+int pado_server_replay(pado_server *s, uint64_t nreq, const double *arrival_s,
+                       const uint32_t *index_id, const uint64_t *k, const uint64_t *pair_off,
+                       const uint32_t *a, const uint32_t *b, uint8_t *out8, int16_t *out16,
+                       uint32_t mode, double *latency_s);
+void pado_server_destroy(pado_server *s);
 
 /* Enable (1) or disable (0) per-kernel timing: while enabled every launch is
  * bracketed by CUDA events on its stream and hot kernels count their

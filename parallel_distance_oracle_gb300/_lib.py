@@ -29,6 +29,12 @@ class Info(C.Structure):
                 ("device_bytes", C.c_uint64), ("levels", C.c_uint32), ("batches", C.c_uint32)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("requests", C.c_uint64), ("batches", C.c_uint64), ("pairs", C.c_uint64),
+                ("max_batch_pairs", C.c_uint64), ("admissions", C.c_uint64), ("evictions", C.c_uint64),
+                ("resident_bytes", C.c_uint64), ("resident_indexes", C.c_uint32), ("pad", C.c_uint32)]
+
+
 def _load() -> C.CDLL:
     lib_path: Path = _build.LIB
     if not _build.up_to_date():
@@ -47,6 +53,8 @@ def _load() -> C.CDLL:
         "pado_version": (C.c_char_p, []),
         "pado_unw_build": (C.c_int, [u32, vp, vp, vp, u32, u32, P(vp)]),
         "pado_unw_build_ranked": (C.c_int, [u32, vp, vp, u32, u32, P(vp)]),
+        "pado_unw_build_many": (C.c_int, [u32, vp, vp, vp, vp, u32, u32, vp]),
+        "pado_unw_tune_batch": (C.c_int, [u32, vp, vp, vp, vp, u32, vp, u32, u32, P(u32), vp]),
         "pado_w_build": (C.c_int, [u32, vp, vp, vp, vp, u32, P(vp)]),
         "pado_w_build_ranked": (C.c_int, [u32, vp, vp, vp, u32, P(vp)]),
         "pado_set_order": (C.c_int, [vp, vp]),
@@ -60,6 +68,13 @@ def _load() -> C.CDLL:
         "pado_load": (C.c_int, [C.c_char_p, u32, P(vp)]),
         "pado_query_noalloc": (C.c_int, [vp, u64, vp, vp, vp]),
         "pado_kernel_launches": (u64, []),
+        "pado_server_create": (C.c_int, [u64, u32, u32, P(vp)]),
+        "pado_server_add": (C.c_int, [vp, vp, P(u32)]),
+        "pado_server_submit": (C.c_int, [vp, u32, u64, vp, vp, vp, P(u64)]),
+        "pado_server_wait": (C.c_int, [vp, u64, C.c_double, P(C.c_double)]),
+        "pado_server_get_stats": (C.c_int, [vp, P(ServerStats)]),
+        "pado_server_replay": (C.c_int, [vp, u64, vp, vp, vp, vp, vp, vp, vp, vp, u32, vp]),
+        "pado_server_destroy": (None, [vp]),
         "pado_profile": (C.c_int, [C.c_int]),
         "pado_profile_read": (C.c_size_t, [C.c_char_p, C.c_size_t, C.c_int]),
     }
@@ -75,9 +90,11 @@ lib = _load()
 # Every symbol include/pado_gpu.h declares (checked by the CPU test suite).
 EXPORTED = [
     "pado_last_error", "pado_status_string", "pado_version", "pado_unw_build", "pado_unw_build_ranked",
+    "pado_unw_build_many", "pado_unw_tune_batch",
     "pado_w_build", "pado_w_build_ranked", "pado_set_order", "pado_free", "pado_get_info", "pado_export",
     "pado_import", "pado_query", "pado_query_device", "pado_query_noalloc", "pado_store", "pado_load",
-    "pado_kernel_launches",
+    "pado_kernel_launches", "pado_server_create", "pado_server_add", "pado_server_submit", "pado_server_wait",
+    "pado_server_get_stats", "pado_server_replay", "pado_server_destroy",
     "pado_profile", "pado_profile_read",
 ]
 

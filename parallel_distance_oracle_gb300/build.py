@@ -20,7 +20,8 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libpado_gpu.so"
-SOURCES = ["capi.cu", "query.cu", "bp.cu", "unw.cu", "weighted.cu", "profile.cu", "noalloc.cu"]
+SOURCES = ["capi.cu", "query.cu", "bp.cu", "unw.cu", "unw_many.cu", "weighted.cu", "profile.cu", "noalloc.cu",
+           "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -224,42 +224,63 @@ __global__ void bp_empty_slots_kernel(uint32_t n, uint32_t K, uint32_t i0, uint8
 
 }  // namespace
 
-BpResult bp_label(const HostGraph &hg, const DevGraph &g, uint32_t K, std::vector<uint8_t> &used,
-                  uint8_t *d_bpd, uint64_t *d_bps, cudaStream_t s)
+void bp_select(const HostGraph &hg, uint32_t lo, uint32_t hi, uint32_t K, std::vector<uint8_t> &used,
+               std::vector<std::vector<BpSeed>> &seeds)
 {
-    BpResult res;
-    const uint32_t n = hg.n;
-    if (K == 0 || n == 0) return res;
-
-    // Root and neighbour selection for every slot, in the reference's order.
-    struct Seed { uint32_t v, lvl; uint64_t bits; };
-    std::vector<std::vector<Seed>> seeds;
-    uint32_t r = 0, nroots = 0;
+    // Root and neighbour selection for every slot, in the reference's order
+    // (pado_unw_unv_unp.h:284-326), restricted to the ids [lo, hi).
+    if (seeds.size() < K) seeds.resize(K);
+    uint32_t r = lo;
     for (uint32_t i = 0; i < K; ++i) {
-        while (r < n && used[r]) ++r;
-        if (r == n) break;
+        while (r < hi && used[r]) ++r;
+        if (r == hi) break;
         used[r] = 1;
-        std::vector<Seed> sd{{r, 0, 0}};
+        seeds[i].push_back({r, 0, 0});
         int ns = 0;
         for (uint32_t k = hg.off[r + 1]; k > hg.off[r]; --k) {
             const uint32_t v = hg.adj[k - 1];
             if (!used[v]) {
                 used[v] = 1;
-                sd.push_back({v, 1, 1ULL << ns});
+                seeds[i].push_back({v, 1, 1ULL << ns});
                 if (++ns == 64) break;
             }
         }
-        seeds.push_back(std::move(sd));
-        ++nroots;
     }
+}
+
+BpResult bp_label(const HostGraph &hg, const DevGraph &g, uint32_t K, std::vector<uint8_t> &used,
+                  uint8_t *d_bpd, uint64_t *d_bps, cudaStream_t s)
+{
+    std::vector<std::vector<BpSeed>> seeds;
+    if (K) bp_select(hg, 0, hg.n, K, used, seeds);
+    return bp_run(hg, g, K, seeds, d_bpd, d_bps, s);
+}
+
+BpResult bp_run(const HostGraph &hg, const DevGraph &g, uint32_t K, const std::vector<std::vector<BpSeed>> &seeds,
+                uint8_t *d_bpd, uint64_t *d_bps, cudaStream_t s)
+{
+    BpResult res;
+    const uint32_t n = hg.n;
+    if (K == 0 || n == 0) return res;
+    // slots [0, nroots) have a root in at least one graph; a graph with fewer
+    // roots gets unreached (255, empty) rows in its remaining slots, which is
+    // what the reference stores for a slot without a root (:288-292).
+    uint32_t nroots = 0;
+    while (nroots < std::min<size_t>(K, seeds.size()) && !seeds[nroots].empty()) ++nroots;
 
     const uint32_t gsize = std::min<uint32_t>(GROUP, std::max<uint32_t>(nroots, 1));
     DBuf<uint32_t> lvl((uint64_t)gsize * n), cnts(8), status(1);
     DBuf<uint64_t> sm1((uint64_t)gsize * n), s0((uint64_t)gsize * n);
     DBuf<uint64_t> fl0((uint64_t)gsize * n), fl1((uint64_t)gsize * n), fh0((uint64_t)gsize * n),
         fh1((uint64_t)gsize * n);
-    DBuf<uint32_t> seed_slot(GROUP * 65), seed_v(GROUP * 65), seed_l(GROUP * 65);
-    DBuf<uint64_t> seed_b(GROUP * 65);
+    size_t max_seeds = 1;
+    for (uint32_t i = 0; i < nroots; i += gsize) {
+        size_t c = 0;
+        for (uint32_t j = i; j < std::min(nroots, i + gsize); ++j) c += seeds[j].size();
+        max_seeds = std::max(max_seeds, c);
+    }
+    DBuf<uint32_t> seed_slot(max_seeds), seed_v(max_seeds), seed_l(max_seeds);
+    DBuf<uint64_t> seed_b(max_seeds);
     status.fill_bytes(0, s);
     uint32_t *h_cnt = nullptr;
     PADO_CUDA(cudaMallocHost((void **)&h_cnt, 8 * sizeof(uint32_t)));
@@ -277,7 +298,7 @@ BpResult bp_label(const HostGraph &hg, const DevGraph &g, uint32_t K, std::vecto
             std::vector<uint32_t> ss, sv, sl;
             std::vector<uint64_t> sb, f0l, f0h, f1l, f1h;
             for (uint32_t j = 0; j < slots; ++j) {
-                for (const Seed &x : seeds[g0 + j]) {
+                for (const BpSeed &x : seeds[g0 + j]) {
                     ss.push_back(j);
                     sv.push_back(x.v);
                     sl.push_back(x.lvl);

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <numeric>
 #include <thread>
 
 #include "pado_internal.cuh"
@@ -18,6 +19,14 @@ struct pado_index {
     pado::DBuf<uint8_t> bpd;     // n * K, rank-indexed
     pado::DBuf<uint64_t> bps;    // n * K * 2
     pado_info info{};
+    // page-locked copies while the device arrays are offloaded
+    bool offloaded = false;
+    struct Host {
+        pado::HBuf<uint32_t> rank, hub;
+        pado::HBuf<uint64_t> off, bps;
+        pado::HBuf<uint8_t> dist8, bpd;
+        pado::HBuf<int16_t> dist16;
+    } host;
 
     pado::IndexView view() const
     {
@@ -170,11 +179,149 @@ int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t 
     });
 }
 
+// Many graphs laid side by side: graph i relabeled by its rank and shifted to
+// ids [gbase[i], gbase[i+1]).
+struct UnionGraph {
+    pado::HostGraph hg;
+    std::vector<uint32_t> gbase;
+};
+
+UnionGraph union_graph(uint32_t G, const uint32_t *n, const uint64_t *const *off, const uint32_t *const *adj,
+                       const uint32_t *const *rank, const std::vector<uint32_t> &pick)
+{
+    UnionGraph u;
+    u.gbase.assign(pick.size() + 1, 0);
+    uint64_t N = 0, M = 0;
+    for (size_t i = 0; i < pick.size(); ++i) {
+        const uint32_t gi = pick[i];
+        PADO_CHECK(gi < G, PADO_E_ARG, "graph index out of range");
+        PADO_CHECK(off[gi] != nullptr, PADO_E_ARG, "null offsets");
+        N += n[gi];
+        M += n[gi] ? off[gi][n[gi]] : 0;
+        PADO_CHECK(N < (1ull << 32) - 1, PADO_E_ARG, "more than 2^32-2 vertices in all graphs together");
+        PADO_CHECK(M < (1ull << 32), PADO_E_ARG, "more than 2^32-1 adjacency entries in all graphs together");
+        u.gbase[i + 1] = (uint32_t)N;
+    }
+    pado::HostGraph &hg = u.hg;
+    hg.n = (uint32_t)N;
+    hg.off.assign(N + 1, 0);
+    hg.adj.resize(M);
+    std::vector<uint32_t> abase(pick.size() + 1, 0);
+    for (size_t i = 0; i < pick.size(); ++i) abase[i + 1] = abase[i] + (n[pick[i]] ? (uint32_t)off[pick[i]][n[pick[i]]] : 0);
+    // relabel the graphs on the host's cores, several graphs per thread
+    const unsigned T = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    std::vector<std::string> errs(T);
+    for (unsigned t = 0; t < T; ++t)
+        th.emplace_back([&, t] {
+            try {
+                for (size_t i = t; i < pick.size(); i += T) {
+                    const uint32_t gi = pick[i], ng = n[gi], base = u.gbase[i];
+                    check_graph(ng, off[gi], adj[gi]);
+                    if (rank && rank[gi]) check_rank(ng, rank[gi]);
+                    pado::HostGraph one = pado::relabel_host(ng, off[gi], adj[gi], nullptr, rank ? rank[gi] : nullptr);
+                    for (uint32_t v = 0; v < ng; ++v) hg.off[base + v + 1] = abase[i] + one.off[v + 1];
+                    for (size_t k = 0; k < one.adj.size(); ++k) hg.adj[abase[i] + k] = one.adj[k] + base;
+                }
+            } catch (const std::exception &e) {
+                errs[t] = e.what();
+            }
+        });
+    for (auto &x : th) x.join();
+    for (auto &e : errs) PADO_CHECK(e.empty(), PADO_E_ARG, e);
+    return u;
+}
+
+// BP rows and batched labels of a union, all on the device.
+struct ManyRun {
+    pado::DevGraph g;
+    pado::DBuf<uint8_t> bpd;
+    pado::DBuf<uint64_t> bps;
+    std::vector<uint8_t> used;
+    float bp_ms = 0.f;
+    uint32_t bp_levels = 0;
+};
+
+void many_bp(const UnionGraph &u, uint32_t K, ManyRun &r, cudaStream_t s)
+{
+    const uint32_t N = u.hg.n;
+    upload_graph(u.hg, r.g, false, s);
+    r.used.assign(N, 0);
+    r.bpd.alloc(std::max<uint64_t>((uint64_t)N * K, 1));
+    r.bps.alloc(std::max<uint64_t>((uint64_t)N * K * 2, 1));
+    std::vector<std::vector<pado::BpSeed>> seeds;
+    if (K)
+        for (size_t i = 0; i + 1 < u.gbase.size(); ++i) pado::bp_select(u.hg, u.gbase[i], u.gbase[i + 1], K, r.used, seeds);
+    pado::BpResult bp = pado::bp_run(u.hg, r.g, K, seeds, r.bpd.p, r.bps.p, s);
+    r.bp_ms = bp.ms;
+    r.bp_levels = bp.levels;
+}
+
 }  // namespace
 
 namespace pado {
 
 int set_error(int code, const std::string &msg) { return fail(code, msg); }
+
+bool index_resident(const pado_index *h) { return !h->offloaded; }
+uint64_t index_device_bytes(const pado_index *h) { return h->info.device_bytes; }
+
+namespace {
+template <typename T>
+void to_host(DBuf<T> &d, HBuf<T> &hb, cudaStream_t s)
+{
+    hb.alloc(d.n);
+    d.download(hb.p, d.n, s);
+}
+}  // namespace
+
+void index_offload(pado_index *h, cudaStream_t s)
+{
+    if (h->offloaded) return;
+    auto &H = h->host;
+    to_host(h->rank, H.rank, s);
+    to_host(h->store.off, H.off, s);
+    to_host(h->store.hub, H.hub, s);
+    to_host(h->store.dist8, H.dist8, s);
+    to_host(h->store.dist16, H.dist16, s);
+    to_host(h->bpd, H.bpd, s);
+    to_host(h->bps, H.bps, s);
+    PADO_CUDA(cudaStreamSynchronize(s));
+    h->rank.release();
+    h->store.off.release();
+    h->store.hub.release();
+    h->store.dist8.release();
+    h->store.dist16.release();
+    h->bpd.release();
+    h->bps.release();
+    h->offloaded = true;
+}
+
+void index_reload(pado_index *h, cudaStream_t s)
+{
+    if (!h->offloaded) return;
+    auto &H = h->host;
+    auto back = [&](auto &hb, auto &d) {
+        d.alloc(hb.n);
+        d.upload(hb.p, hb.n, s);
+    };
+    back(H.rank, h->rank);
+    back(H.off, h->store.off);
+    back(H.hub, h->store.hub);
+    back(H.dist8, h->store.dist8);
+    back(H.dist16, h->store.dist16);
+    back(H.bpd, h->bpd);
+    back(H.bps, h->bps);
+    PADO_CUDA(cudaStreamSynchronize(s));
+    H.rank.release();
+    H.off.release();
+    H.hub.release();
+    H.dist8.release();
+    H.dist16.release();
+    H.bpd.release();
+    H.bps.release();
+    h->offloaded = false;
+}
 IndexView index_view(const pado_index *h) { return h->view(); }
 uint32_t index_kind(const pado_index *h) { return h->kind; }
 int index_device(const pado_index *h) { return h->device; }
@@ -273,9 +420,129 @@ int pado_w_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, co
     return build_common(true, n, off, adj, w, nullptr, 0, batch, out);
 }
 
+int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *off, const uint32_t *const *adj,
+                        const uint32_t *const *rank, uint32_t bp_roots, uint32_t batch, pado_index **out)
+{
+    if (!out || (G && (!n || !off || !adj))) return fail(PADO_E_ARG, "null argument");
+    for (uint32_t i = 0; i < G; ++i) out[i] = nullptr;
+    std::vector<std::unique_ptr<pado_index>> hs(G);
+    const int st = guarded([&] {
+        PADO_CHECK(G >= 1 && G <= 65535, PADO_E_ARG, "between 1 and 65535 graphs");
+        PADO_CHECK(batch >= 1 && batch <= pado::MAX_BATCH, PADO_E_ARG, "batch size must be in [1, 2048]");
+        PADO_CHECK(bp_roots <= pado::MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
+        std::vector<uint32_t> pick(G);
+        std::iota(pick.begin(), pick.end(), 0u);
+        UnionGraph u = union_graph(G, n, off, adj, rank, pick);
+        int dev = 0;
+        PADO_CUDA(cudaGetDevice(&dev));
+        cudaStream_t s;
+        PADO_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
+        ManyRun r;
+        many_bp(u, bp_roots, r, s);
+        pado::LabelStore all;
+        pado::LabelRun run = pado::unw_label_many(r.g, u.gbase, bp_roots, batch, r.used, r.bpd.p, r.bps.p, all, s);
+        const uint32_t N = u.hg.n;
+        std::vector<uint64_t> fo(N + 1);
+        all.off.download(fo.data(), N + 1, s);
+        PADO_CUDA(cudaStreamSynchronize(s));
+        const uint32_t K = bp_roots;
+        for (uint32_t i = 0; i < G; ++i) {
+            const uint32_t base = u.gbase[i], ng = n[i];
+            std::unique_ptr<pado_index> h(new pado_index);
+            h->device = dev;
+            h->kind = PADO_UNWEIGHTED;
+            h->n = ng;
+            h->K = K;
+            h->B = batch;
+            if (rank && rank[i]) {
+                h->rank.alloc(std::max<uint32_t>(ng, 1));
+                h->rank.upload(rank[i], ng, s);
+            }
+            const uint64_t l0 = fo[base], tot = fo[base + ng] - l0;
+            std::vector<uint64_t> lo(ng + 1);
+            for (uint32_t v = 0; v <= ng; ++v) lo[v] = fo[base + v] - l0;
+            h->store.total = tot;
+            h->store.off.alloc(ng + 1);
+            h->store.off.upload(lo.data(), ng + 1, s);
+            h->store.hub.alloc(std::max<uint64_t>(tot, 1));
+            h->store.dist8.alloc(std::max<uint64_t>(tot, 1));
+            if (tot) {
+                PADO_CUDA(cudaMemcpyAsync(h->store.hub.p, all.hub.p + l0, tot * 4, cudaMemcpyDeviceToDevice, s));
+                PADO_CUDA(cudaMemcpyAsync(h->store.dist8.p, all.dist8.p + l0, tot, cudaMemcpyDeviceToDevice, s));
+            }
+            h->bpd.alloc(std::max<uint64_t>((uint64_t)ng * K, 1));
+            h->bps.alloc(std::max<uint64_t>((uint64_t)ng * K * 2, 1));
+            if ((uint64_t)ng * K) {
+                PADO_CUDA(cudaMemcpyAsync(h->bpd.p, r.bpd.p + (uint64_t)base * K, (uint64_t)ng * K,
+                                          cudaMemcpyDeviceToDevice, s));
+                PADO_CUDA(cudaMemcpyAsync(h->bps.p, r.bps.p + (uint64_t)base * K * 2, (uint64_t)ng * K * 16,
+                                          cudaMemcpyDeviceToDevice, s));
+            }
+            // lo[] must stay alive until its upload has run
+            PADO_CUDA(cudaStreamSynchronize(s));
+            h->info.n = ng;
+            h->info.kind = PADO_UNWEIGHTED;
+            h->info.bp_roots = K;
+            h->info.batch = batch;
+            h->info.num_labels = tot;
+            h->info.batches = (uint32_t)(((uint64_t)ng + batch - 1) / batch);
+            h->info.levels = run.levels + r.bp_levels;
+            h->info.bp_seconds = r.bp_ms * 1e-3;
+            h->info.build_seconds = (r.bp_ms + run.ms) * 1e-3;
+            h->info.device_bytes = h->device_bytes();
+            hs[i] = std::move(h);
+        }
+    });
+    if (st == PADO_OK)
+        for (uint32_t i = 0; i < G; ++i) out[i] = hs[i].release();
+    return st;
+}
+
+int pado_unw_tune_batch(uint32_t G, const uint32_t *n, const uint64_t *const *off, const uint32_t *const *adj,
+                        const uint32_t *const *rank, uint32_t bp_roots, const uint32_t *candidates,
+                        uint32_t ncand, uint32_t sample, uint32_t *best, float *ms)
+{
+    if (!best || !candidates || !ncand || (G && (!n || !off || !adj))) return fail(PADO_E_ARG, "null argument");
+    return guarded([&] {
+        PADO_CHECK(G >= 1 && G <= 65535, PADO_E_ARG, "between 1 and 65535 graphs");
+        PADO_CHECK(bp_roots <= pado::MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
+        for (uint32_t c = 0; c < ncand; ++c)
+            PADO_CHECK(candidates[c] >= 1 && candidates[c] <= pado::MAX_BATCH, PADO_E_ARG,
+                       "batch size must be in [1, 2048]");
+        // sample: graphs evenly spaced in size order, both ends included
+        std::vector<uint32_t> bysize(G);
+        std::iota(bysize.begin(), bysize.end(), 0u);
+        std::stable_sort(bysize.begin(), bysize.end(), [&](uint32_t a, uint32_t b) { return n[a] < n[b]; });
+        const uint32_t k = sample == 0 || sample >= G ? G : sample;
+        std::vector<uint32_t> pick;
+        for (uint32_t i = 0; i < k; ++i) pick.push_back(bysize[k == 1 ? G - 1 : (uint64_t)i * (G - 1) / (k - 1)]);
+        std::sort(pick.begin(), pick.end());
+        pick.erase(std::unique(pick.begin(), pick.end()), pick.end());
+        UnionGraph u = union_graph(G, n, off, adj, rank, pick);
+        cudaStream_t s;
+        PADO_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
+        ManyRun r;
+        many_bp(u, bp_roots, r, s);  // BP rows do not depend on the batch size
+        float best_ms = 0.f;
+        for (uint32_t c = 0; c < ncand; ++c) {
+            pado::LabelStore st;
+            pado::LabelRun run = pado::unw_label_many(r.g, u.gbase, bp_roots, candidates[c], r.used, r.bpd.p, r.bps.p,
+                                                      st, s);
+            if (ms) ms[c] = run.ms;
+            if (c == 0 || run.ms < best_ms) {
+                best_ms = run.ms;
+                *best = candidates[c];
+            }
+        }
+    });
+}
+
 int pado_set_order(pado_index *h, const uint32_t *rank)
 {
     if (!h) return fail(PADO_E_ARG, "null index");
+    if (h->offloaded) return fail(PADO_E_STATE, "index is offloaded to host memory by a serving loop");
     return guarded([&] {
         check_rank(h->n, rank);
         PADO_CUDA(cudaSetDevice(h->device));
@@ -303,6 +570,7 @@ int pado_get_info(const pado_index *h, pado_info *info)
 int pado_export(const pado_index *h, uint64_t *off, uint32_t *hub, void *dist, uint8_t *bp_dist, uint64_t *bp_sets)
 {
     if (!h || !off || (h->store.total && (!hub || !dist))) return fail(PADO_E_ARG, "null argument");
+    if (h->offloaded) return fail(PADO_E_STATE, "index is offloaded to host memory by a serving loop");
     return guarded([&] {
         PADO_CUDA(cudaSetDevice(h->device));
         const uint32_t n = h->n, K = h->K;
@@ -400,6 +668,7 @@ int pado_import(uint32_t kind, uint32_t n, uint32_t bp_roots, const uint64_t *of
 int pado_query_device(pado_index *h, uint64_t k, const uint32_t *d_a, const uint32_t *d_b, void *d_out, void *stream)
 {
     if (!h || (k && (!d_a || !d_b || !d_out))) return fail(PADO_E_ARG, "null argument");
+    if (h->offloaded) return fail(PADO_E_STATE, "index is offloaded to host memory by a serving loop");
     return guarded([&] {
         PADO_CUDA(cudaSetDevice(h->device));
         cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -413,6 +682,7 @@ int pado_query_device(pado_index *h, uint64_t k, const uint32_t *d_a, const uint
 int pado_query(pado_index *h, uint64_t k, const uint32_t *a, const uint32_t *b, void *out)
 {
     if (!h || (k && (!a || !b || !out))) return fail(PADO_E_ARG, "null argument");
+    if (h->offloaded) return fail(PADO_E_STATE, "index is offloaded to host memory by a serving loop");
     if (!k) return PADO_OK;
     return guarded([&] {
         PADO_CUDA(cudaSetDevice(h->device));
@@ -443,6 +713,7 @@ int pado_query(pado_index *h, uint64_t k, const uint32_t *a, const uint32_t *b, 
 int pado_store(const pado_index *h, const char *path)
 {
     if (!h || !path) return fail(PADO_E_ARG, "null argument");
+    if (h->offloaded) return fail(PADO_E_STATE, "index is offloaded to host memory by a serving loop");
     const uint32_t n = h->n, K = h->K;
     const uint64_t tot = h->store.total;
     std::vector<uint64_t> off(n + 1);

@@ -70,6 +70,8 @@ int pado_query_noalloc(pado_index *h, uint64_t k, const uint32_t *a, const uint3
                                                std::to_string(NOALLOC_MAX_PAIRS) +
                                                " pairs; split the batch or use pado_query");
     if (!k) return PADO_OK;
+    if (!pado::index_resident(h))
+        return pado::set_error(PADO_E_STATE, "index is offloaded to host memory by a serving loop");
     const int dev = pado::index_device(h);
     cudaError_t e = cudaSetDevice(dev);
     if (e != cudaSuccess) return pado::set_error(PADO_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));

@@ -82,6 +82,36 @@ struct DBuf {
     }
 };
 
+// Owning page-locked host buffer (DMA-able without a driver-side staging copy).
+template <typename T>
+struct HBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    HBuf() = default;
+    explicit HBuf(size_t count) { alloc(count); }
+    HBuf(const HBuf &) = delete;
+    HBuf &operator=(const HBuf &) = delete;
+    HBuf(HBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    HBuf &operator=(HBuf &&o) noexcept
+    {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~HBuf() { release(); }
+    void alloc(size_t count)
+    {
+        release();
+        if (count) PADO_CUDA(cudaMallocHost((void **)&p, count * sizeof(T)));
+        n = count;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
 inline unsigned grid_for(uint64_t items, unsigned block, unsigned cap = 152u * 64u)
 {
     uint64_t g = (items + block - 1) / block;

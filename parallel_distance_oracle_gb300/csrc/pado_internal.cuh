@@ -56,6 +56,20 @@ struct BpResult {
 BpResult bp_label(const HostGraph &hg, const DevGraph &g, uint32_t K, std::vector<uint8_t> &used,
                   uint8_t *d_bpd, uint64_t *d_bps, cudaStream_t s);
 
+// The two halves of bp_label.  bp_select appends, for BP slot i, the root and
+// selected neighbours of the graph occupying ids [lo, hi) to seeds[i] and
+// marks them used; called once per graph of a union it gives every graph its
+// own slot roots.  bp_run labels all slots over the (union) graph: graphs are
+// disjoint, so one BFS per slot serves every graph's root at once.
+struct BpSeed {
+    uint32_t v, lvl;
+    uint64_t bits;
+};
+void bp_select(const HostGraph &hg, uint32_t lo, uint32_t hi, uint32_t K, std::vector<uint8_t> &used,
+               std::vector<std::vector<BpSeed>> &seeds);
+BpResult bp_run(const HostGraph &hg, const DevGraph &g, uint32_t K, const std::vector<std::vector<BpSeed>> &seeds,
+                uint8_t *d_bpd, uint64_t *d_bps, cudaStream_t s);
+
 // Final label store produced by a labeler (rank-indexed, sorted by hub).
 struct LabelStore {
     DBuf<uint64_t> off;
@@ -75,6 +89,14 @@ struct LabelRun {
 LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<uint8_t> &used,
                    const uint8_t *d_bpd, const uint64_t *d_bps, LabelStore &out, cudaStream_t s);
 
+// unw_many.cu: the same labeling for many independent graphs at once.  `g` is
+// the disjoint union, graph i owning ids [gbase[i], gbase[i+1]); every graph
+// runs its own batch sequence, all advancing one level per step of one
+// persistent launch.  `out` is indexed by union id with graph-local hubs.
+LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, uint32_t K, uint32_t B,
+                        const std::vector<uint8_t> &used, const uint8_t *d_bpd, const uint64_t *d_bps,
+                        LabelStore &out, cudaStream_t s);
+
 // weighted.cu: batched pruned relaxation (pado_weighted_unv_unp.h:281-1526).
 LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s);
 
@@ -84,5 +106,14 @@ int set_error(int code, const std::string &msg);
 IndexView index_view(const pado_index *h);
 uint32_t index_kind(const pado_index *h);
 int index_device(const pado_index *h);
+
+// Residency of an index's device arrays, for the serving loop's admission
+// control: offload copies them to page-locked host memory and frees the
+// device copies; reload brings them back (both complete before returning).
+// Queries on an offloaded index fail with PADO_E_STATE.
+bool index_resident(const pado_index *h);
+uint64_t index_device_bytes(const pado_index *h);
+void index_offload(pado_index *h, cudaStream_t s);
+void index_reload(pado_index *h, cudaStream_t s);
 
 }  // namespace pado

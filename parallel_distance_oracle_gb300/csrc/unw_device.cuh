@@ -1,0 +1,869 @@
+// unw_device.cuh -- device side of the batched pruned-BFS labeling, shared by
+// the one-graph driver (unw.cu) and the many-graph driver (unw_many.cu).
+//
+// Restates the batched vertex-centric labeling of the reference
+// (includes/pado_unw_unv_unp.h:425-1118; OpenMP variant
+// pado_unw_unv_para.201912311607.parallel_bp_labeling.h:848-1737); the
+// algorithm and its device mapping are described at the top of unw.cu.  Every
+// phase below is a grid-stride __device__ function so that it can run inside a
+// plain kernel or inside a persistent cooperative loop.
+#pragma once
+
+#include "pado_internal.cuh"
+
+namespace pado {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int SMALL_CAP = 256;                 // labels with d < iter staged in smem
+constexpr uint32_t HEAVY_DEG = 2048;           // tails this large are processed by a block
+
+struct UnwDev {
+    uint32_t n, K, B, words;
+    const uint32_t *off;
+    const uint32_t *adj;
+    const uint8_t *used;
+    const uint8_t *bpd;
+    const uint64_t *bps;
+    uint32_t *pool_hub;
+    uint8_t *pool_dist;
+    unsigned long long pool_cap;
+    unsigned long long *pool_top;
+    uint64_t *lab_off;
+    uint32_t *lab_len;
+    uint32_t *lab_cap;
+    uint64_t *last_pos[2];
+    uint32_t *last_cnt[2];
+    uint32_t *last_min[2];
+    uint32_t *act_stamp[2];  // by level parity: level id at which the vertex gained labels
+    uint32_t *tail_stamp;
+    uint32_t *ind;        // n * words
+    uint32_t *ind_stamp;  // batch + 1 when the row is valid
+    uint8_t *dm;          // B * n
+    uint32_t *status;
+    unsigned long long *work;  // algorithmic-byte counters (profiling only)
+};
+
+// Per-graph state when many graphs are labeled together in one union id space:
+// graph g owns ids [base, base + n); its batch b holds the roots of
+// [base + b*B, base + (b+1)*B) and its dist_matrix is a [B][n] block at
+// dm + dm_off, entry (root idx, hub h) at idx * n + (h - base).
+struct GDesc {
+    uint32_t base, n;        // id range
+    uint32_t nb;             // number of batches
+    uint32_t b;              // current batch
+    uint32_t s, e;           // current batch's id range [s, e)
+    uint32_t iter;           // level computed in the current step
+    uint32_t state;          // GS_* below
+    uint32_t fcnt[2];        // vertices that gained labels, by step parity
+    uint32_t roff, nr;       // current batch's roots: broots[roff, roff + nr)
+    uint32_t bfirst;         // this graph's entries in the per-batch root counts
+    uint32_t pad;
+    uint64_t dm_off;         // offset of the graph's dist_matrix block
+};
+enum : uint32_t { GS_START = 0, GS_LEVEL = 1, GS_DONE = 2 };
+
+// Graph descriptors change between the steps of a persistent launch (written
+// by one warp, read by every SM), so they are read at L2 (ld.global.cg), never
+// from a possibly stale L1 line.
+__device__ __forceinline__ uint32_t gd_u32(const uint32_t &f) { return __ldcg(&f); }
+__device__ __forceinline__ uint64_t gd_u64(const uint64_t &f)
+{
+    return (uint64_t)__ldcg(reinterpret_cast<const unsigned long long *>(&f));
+}
+
+__device__ __forceinline__ uint32_t warp_min_u32(uint32_t v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+
+// Reserve room for `need` entries in v's list; relocates (warp-cooperative
+// copy) when the slot is too small.  Returns false, with nothing changed
+// except pool_top, when the pool is exhausted.
+__device__ __forceinline__ bool warp_reserve(const UnwDev &d, uint32_t v, uint32_t need, uint64_t &base, int lane)
+{
+    const uint32_t len = d.lab_len[v], cap = d.lab_cap[v];
+    base = d.lab_off[v];
+    if (need <= cap) return true;
+    uint32_t ncap = max(max(2u * cap, need), 8u);
+    ncap = (ncap + 7u) & ~7u;
+    unsigned long long pos = 0;
+    if (lane == 0) pos = atomicAdd(d.pool_top, (unsigned long long)ncap);
+    pos = __shfl_sync(FULL, pos, 0);
+    if (pos + ncap > d.pool_cap) return false;
+    for (uint32_t j = lane; j < len; j += 32) {
+        d.pool_hub[pos + j] = d.pool_hub[base + j];
+        d.pool_dist[pos + j] = d.pool_dist[base + j];
+    }
+    __syncwarp();
+    if (lane == 0) {
+        d.lab_off[v] = pos;
+        d.lab_cap[v] = ncap;
+    }
+    base = pos;
+    return true;
+}
+
+// Batch start: self label (r, 0) for every non-BP root, indicator row with
+// the root's own bit, active at level stamp lid0 (pado_unw_unv_unp.h:425-491).
+// With gmap set, each root's batch (start s, id b) is its graph's current one.
+__device__ void root_init_phase(const UnwDev &d, const uint32_t *roots, uint32_t nroots, uint32_t s, uint32_t b,
+                                uint32_t lid0, uint32_t *front, uint32_t *front_cnt, uint32_t *retry,
+                                uint32_t *retry_cnt, const GDesc *gd = nullptr, const uint16_t *gmap = nullptr)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const int p = lid0 & 1;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nroots; q += nw) {
+        const uint32_t r = roots[q];
+        uint64_t base;
+        if (!warp_reserve(d, r, d.lab_len[r] + 1, base, lane)) {
+            if (lane == 0) {
+                atomicOr(d.status, ST_POOL_RETRY);
+                retry[atomicAdd(retry_cnt, 1u)] = r;
+            }
+            continue;
+        }
+        const uint32_t len = d.lab_len[r];
+        uint32_t rs = s, rb = b;
+        if (gmap) {
+            const GDesc &x = gd[gmap[r]];
+            rs = gd_u32(x.s);
+            rb = gd_u32(x.b);
+        }
+        const uint32_t idx = r - rs;
+        for (uint32_t w = lane; w < d.words; w += 32)
+            d.ind[(uint64_t)r * d.words + w] = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
+        if (lane == 0) {
+            d.pool_hub[base + len] = r;
+            d.pool_dist[base + len] = 0;
+            d.lab_len[r] = len + 1;
+            d.last_pos[p][r] = base + len;
+            d.last_cnt[p][r] = 1;
+            d.last_min[p][r] = r;
+            d.act_stamp[p][r] = lid0;
+            d.ind_stamp[r] = rb + 1;
+            front[atomicAdd(front_cnt, 1u)] = r;
+        }
+    }
+}
+
+// dist_matrix rows of the batch roots: fill from their labels (value = d) or
+// reset to 255 (pado_unw_unv_unp.h:492-526 and :780-816).
+// With gmap set, root r's row is (r - base) % B of its graph's block (batches
+// are B-aligned within a graph, so this is r - s of the batch r belongs to).
+__device__ void dm_rows_phase(const UnwDev &d, const uint32_t *roots, uint32_t nroots, uint32_t s, int fill,
+                              const GDesc *gd = nullptr, const uint16_t *gmap = nullptr)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nroots; q += nw) {
+        const uint32_t r = roots[q];
+        uint8_t *row;
+        uint32_t hb = 0;
+        if (gmap) {
+            const GDesc &x = gd[gmap[r]];
+            hb = x.base;
+            row = d.dm + x.dm_off + (uint64_t)((r - hb) % d.B) * x.n;  // fields fixed for the launch
+        } else {
+            row = d.dm + (uint64_t)(r - s) * d.n;
+        }
+        const uint64_t base = d.lab_off[r];
+        const uint32_t len = d.lab_len[r];
+        for (uint32_t j = lane; j < len; j += 32)
+            row[d.pool_hub[base + j] - hb] = fill ? d.pool_dist[base + j] : U8_INF;
+    }
+}
+
+// Tail marking: for each active head, neighbours t (descending) with
+// t > min(root of its last group) that are not BP vertices.
+__device__ void mark_phase(const UnwDev &d, const uint32_t *front, uint32_t cnt, uint32_t lid_cur, uint32_t *tails,
+                           uint32_t *tails_cnt, uint32_t *htails, uint32_t *htails_cnt)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const int pp = (lid_cur - 1) & 1;
+    unsigned long long bytes = 0;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw) {
+        const uint32_t h = front[q];
+        const uint32_t mn = d.last_min[pp][h];
+        const uint32_t e_end = d.off[h + 1];
+        bytes += 16;  // front entry, last_min, offsets
+        for (uint32_t e0 = d.off[h]; e0 < e_end; e0 += 32) {
+            const uint32_t e = e0 + lane;
+            const bool in = e < e_end;
+            const uint32_t t = in ? d.adj[e] : 0u;
+            const bool ok = in && t > mn;
+            bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
+            bool appended = false;
+            if (ok && !d.used[t] && d.tail_stamp[t] != lid_cur) {
+                if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) {
+                    if (d.off[t + 1] - d.off[t] >= HEAVY_DEG)
+                        htails[atomicAdd(htails_cnt, 1u)] = t;
+                    else
+                        tails[atomicAdd(tails_cnt, 1u)] = t;
+                    appended = true;
+                }
+            }
+            bytes += __popc(__ballot_sync(FULL, appended)) * 8ull;
+            if (__ballot_sync(FULL, in && !ok)) break;  // descending: the rest are smaller
+        }
+    }
+    if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_MARK], bytes);
+}
+
+// Shared-memory layout of the pull kernel, carved from dynamic shared memory
+// by batch size: 8 per-warp regions for light tails, aliased by one
+// block-wide region for heavy tails (the two phases do not overlap).
+constexpr int PULL_THREADS = 256;
+constexpr int PULL_NW = PULL_THREADS / 32;
+constexpr int HSMALL_CAP = 1024;          // heavy tail: labels with d < iter staged
+
+__host__ __device__ __forceinline__ uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
+
+struct WarpRegion {
+    uint32_t *ind;        // words
+    uint16_t *offered;    // B
+    uint8_t *tbpd;        // 64
+    ulonglong2 *tbps;     // 64
+    uint32_t *sh;         // SMALL_CAP
+    uint8_t *sd;          // SMALL_CAP
+    uint32_t *ctr;        // [0] noff, [1] nsmall
+};
+
+__host__ __device__ __forceinline__ uint32_t warp_region_bytes(uint32_t words, uint32_t B)
+{
+    return align16(words * 4) + align16(B * 2) + 64 + 64 * 16 + SMALL_CAP * 4 + SMALL_CAP + 16;
+}
+
+__host__ __device__ __forceinline__ uint32_t heavy_region_bytes(uint32_t words, uint32_t B)
+{
+    return align16(words * 4) + 2 * align16(B * 2) + 64 + 64 * 16 + HSMALL_CAP * 4 + HSMALL_CAP + 64;
+}
+
+__host__ __device__ __forceinline__ uint32_t pull_smem_bytes(uint32_t words, uint32_t B)
+{
+    const uint32_t l = PULL_NW * warp_region_bytes(words, B), h = heavy_region_bytes(words, B);
+    return l > h ? l : h;
+}
+
+__device__ __forceinline__ WarpRegion warp_region(unsigned char *base, uint32_t words, uint32_t B, int w)
+{
+    unsigned char *p = base + (size_t)w * warp_region_bytes(words, B);
+    WarpRegion r;
+    r.tbps = reinterpret_cast<ulonglong2 *>(p);
+    p += 64 * 16;
+    r.ind = reinterpret_cast<uint32_t *>(p);
+    p += align16(words * 4);
+    r.sh = reinterpret_cast<uint32_t *>(p);
+    p += SMALL_CAP * 4;
+    r.ctr = reinterpret_cast<uint32_t *>(p);
+    p += 16;
+    r.offered = reinterpret_cast<uint16_t *>(p);
+    p += align16(B * 2);
+    r.tbpd = p;
+    p += 64;
+    r.sd = p;
+    return r;
+}
+
+struct HeavyRegion {
+    ulonglong2 *tbps;
+    uint32_t *ind;
+    uint32_t *sh;
+    uint16_t *offered;
+    uint16_t *surv;
+    uint8_t *tbpd;
+    uint8_t *sd;
+    uint32_t *ctr;                   // noff, nsurv, nsmall, nadd, mn, ok, reloc, ncap
+    unsigned long long *base;
+};
+
+__device__ __forceinline__ HeavyRegion heavy_region(unsigned char *p, uint32_t words, uint32_t B)
+{
+    HeavyRegion r;
+    r.tbps = reinterpret_cast<ulonglong2 *>(p);
+    p += 64 * 16;
+    r.base = reinterpret_cast<unsigned long long *>(p);
+    p += 16;
+    r.ctr = reinterpret_cast<uint32_t *>(p);
+    p += 48;
+    r.ind = reinterpret_cast<uint32_t *>(p);
+    p += align16(words * 4);
+    r.sh = reinterpret_cast<uint32_t *>(p);
+    p += HSMALL_CAP * 4;
+    r.offered = reinterpret_cast<uint16_t *>(p);
+    p += align16(B * 2);
+    r.surv = reinterpret_cast<uint16_t *>(p);
+    p += align16(B * 2);
+    r.tbpd = p;
+    p += 64;
+    r.sd = p;
+    return r;
+}
+
+// BP test of one (root, tail) pair on BP root i only.
+__device__ __forceinline__ bool bp_one(uint8_t rd, ulonglong2 rs, uint8_t td, ulonglong2 ts, uint32_t iter)
+{
+    uint32_t x = (uint32_t)rd + (uint32_t)td;
+    if (x - 2u > iter) return false;
+    if (rs.x & ts.x)
+        x -= 2u;
+    else if ((rs.x & ts.y) | (rs.y & ts.x))
+        x -= 1u;
+    return x <= iter;
+}
+
+// Warp-cooperative BP test of candidate root r against the tail's row held in
+// registers (lane i holds BP roots i and i + 32); roots < skip were already
+// tested.  Pruned iff any root covers the pair -- order-independent.
+__device__ __forceinline__ bool bp_covered_warp(const UnwDev &d, uint32_t r, int lane, uint32_t skip, uint8_t td0,
+                                                ulonglong2 ts0, uint8_t td1, ulonglong2 ts1, uint32_t iter)
+{
+    const uint8_t *rd = d.bpd + (uint64_t)r * d.K;
+    const ulonglong2 *rs = reinterpret_cast<const ulonglong2 *>(d.bps + (uint64_t)r * d.K * 2);
+    bool cov = false;
+    const uint32_t i0 = lane, i1 = lane + 32;
+    if (i0 >= skip && i0 < d.K) cov = bp_one(rd[i0], rs[i0], td0, ts0, iter);
+    if (i1 >= skip && i1 < d.K) cov = cov || bp_one(rd[i1], rs[i1], td1, ts1, iter);
+    return __ballot_sync(FULL, cov) != 0;
+}
+
+struct PullArgs {
+    const uint32_t *tails;        // light tails
+    const uint32_t *tails_cnt;
+    const uint32_t *htails;       // heavy tails
+    const uint32_t *htails_cnt;
+    uint32_t s, e_roots, b, iter, lid_cur;
+    uint32_t *front_next;
+    uint32_t *front_next_cnt;
+    uint32_t *retry;
+    uint32_t *retry_cnt;
+    const GDesc *gd = nullptr;       // many-graph labeling: per-graph state ...
+    const uint16_t *gmap = nullptr;  // ... and the graph of each vertex
+    GDesc *gd_mut = nullptr;         // the same array, for the per-graph counters
+};
+
+// The batch a tail belongs to: roots [s, e), batch id b, level iter, and its
+// graph's dist_matrix rows (entry for root idx, hub h: dm[idx * dn + h - base]).
+struct BatchCtx {
+    uint32_t s, e, b, iter, base, dn;
+    uint8_t *dm;
+    uint32_t g;
+};
+
+__device__ __forceinline__ BatchCtx tail_ctx(const UnwDev &d, const PullArgs &a, uint32_t t)
+{
+    if (!a.gmap) return BatchCtx{a.s, a.e_roots, a.b, a.iter, 0u, d.n, d.dm, 0u};
+    const uint32_t g = a.gmap[t];
+    const GDesc &x = a.gd[g];
+    return BatchCtx{gd_u32(x.s), gd_u32(x.e), gd_u32(x.b), gd_u32(x.iter), x.base, x.n, d.dm + x.dm_off, g};
+}
+
+// One heavy tail, processed by the whole block.
+__device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, HeavyRegion &hs,
+                                unsigned long long &bytes)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const BatchCtx bc = tail_ctx(d, a, t);
+    const uint32_t s = bc.s, iter = bc.iter;
+    const int pp = (a.lid_cur - 1) & 1, cp = a.lid_cur & 1;
+    const uint32_t lid_prev = a.lid_cur - 1;
+    const bool valid = d.ind_stamp[t] == bc.b + 1;
+    for (uint32_t x = tid; x < d.words; x += blockDim.x) hs.ind[x] = valid ? d.ind[(uint64_t)t * d.words + x] : 0u;
+    if (tid < 8) hs.ctr[tid] = (tid == 4) ? 0xffffffffu : 0u;
+    if (tid == 0) bytes += 8 + 8ull * d.words;
+    __syncthreads();
+    // (a) first offers from active neighbours, warps striding over the list
+    const uint32_t e_end = d.off[t + 1];
+    for (uint32_t e0 = d.off[t] + 32 * warp; e0 < e_end; e0 += 32 * (blockDim.x >> 5)) {
+        const uint32_t e = e0 + lane;
+        const bool in = e < e_end;
+        const uint32_t h = in ? d.adj[e] : 0u;
+        const bool ge = in && h >= s;
+        const bool act = ge && d.act_stamp[pp][h] == lid_prev;
+        uint32_t mask = __ballot_sync(FULL, act);
+        if (lane == 0) bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull;
+        else { __ballot_sync(FULL, in); __ballot_sync(FULL, ge); }
+        while (mask) {
+            const int src = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const uint32_t hh = __shfl_sync(FULL, h, src);
+            const uint64_t pos = d.last_pos[pp][hh];
+            const uint32_t c = d.last_cnt[pp][hh];
+            if (lane == 0) bytes += 12 + 4ull * c;
+            for (uint32_t j = lane; j < c; j += 32) {
+                const uint32_t r = d.pool_hub[pos + j];
+                if (r < t) {
+                    const uint32_t idx = r - s;
+                    const uint32_t bit = 1u << (idx & 31);
+                    const uint32_t old = atomicOr(&hs.ind[idx >> 5], bit);
+                    if (!(old & bit)) hs.offered[atomicAdd(&hs.ctr[0], 1u)] = (uint16_t)idx;
+                }
+            }
+        }
+        if (__ballot_sync(FULL, in && !ge)) break;  // descending list: the rest are < s
+    }
+    __syncthreads();
+    const uint32_t noff = hs.ctr[0];
+    if (noff == 0) return;  // uniform: nothing changed
+    // (b) BP test: thread per candidate on BP root 0, then warps take the
+    // survivors one at a time over the remaining roots.
+    if (tid == 0) bytes += 17ull * d.K;
+    const ulonglong2 zero2 = make_ulonglong2(0, 0);
+    const uint8_t td0 = lane < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane] : (uint8_t)U8_INF;
+    const uint8_t td1 = lane + 32 < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane + 32] : (uint8_t)U8_INF;
+    const ulonglong2 ts0 = lane < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane] : zero2;
+    const ulonglong2 ts1 =
+        lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
+    const uint8_t tr0d = __shfl_sync(FULL, td0, 0);
+    const ulonglong2 tr0s = make_ulonglong2(__shfl_sync(FULL, ts0.x, 0), __shfl_sync(FULL, ts0.y, 0));
+    for (uint32_t c = tid; c < noff; c += blockDim.x) {
+        const uint16_t idx = hs.offered[c];
+        const uint64_t rr = s + idx;
+        if (d.K == 0 ||
+            !bp_one(d.bpd[rr * d.K], reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K], tr0d, tr0s, iter))
+            hs.surv[atomicAdd(&hs.ctr[1], 1u)] = idx;
+    }
+    __syncthreads();
+    const uint32_t nsurv1 = hs.ctr[1];
+    if (d.K > 1 && nsurv1) {
+        if (tid == 0) hs.ctr[1] = 0;
+        __syncthreads();
+        for (uint32_t c = warp; c < nsurv1; c += blockDim.x >> 5) {
+            const uint16_t idx = hs.surv[c];
+            const bool cov = bp_covered_warp(d, s + idx, lane, 1, td0, ts0, td1, ts1, iter);
+            if (!cov && lane == 0) hs.offered[atomicAdd(&hs.ctr[1], 1u)] = idx;
+        }
+        __syncthreads();
+        // survivors now sit in `offered`; move them back for the distance test
+        const uint32_t ns2 = hs.ctr[1];
+        for (uint32_t c = tid; c < ns2; c += blockDim.x) hs.surv[c] = hs.offered[c];
+        __syncthreads();
+    }
+    const uint32_t nsurv = hs.ctr[1];
+    const uint32_t len = d.lab_len[t];
+    const uint64_t base = d.lab_off[t];
+    // (c) distance test
+    if (nsurv) {
+        for (uint32_t j = tid; j < len; j += blockDim.x) {
+            const uint8_t dd = d.pool_dist[base + j];
+            if (dd < iter) {
+                const uint32_t slot = atomicAdd(&hs.ctr[2], 1u);
+                if (slot < HSMALL_CAP) {
+                    hs.sh[slot] = d.pool_hub[base + j];
+                    hs.sd[slot] = dd;
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t nsmall = hs.ctr[2];
+        if (tid == 0) bytes += 12 + (uint64_t)len + 4ull * min(nsmall, (uint32_t)HSMALL_CAP) + (uint64_t)nsurv * nsmall;
+        for (uint32_t c = tid; c < nsurv; c += blockDim.x) {
+            const uint16_t idx = hs.surv[c];
+            const uint32_t rr = s + idx;
+            const uint8_t *row = bc.dm + (uint64_t)idx * bc.dn;
+            bool keep = true;
+            if (nsmall <= HSMALL_CAP) {
+                for (uint32_t k = 0; k < nsmall; ++k) {
+                    const uint32_t hh = hs.sh[k];
+                    if (hh < rr && (uint32_t)hs.sd[k] + (uint32_t)row[hh - bc.base] <= iter) { keep = false; break; }
+                }
+            } else {
+                for (uint32_t j = 0; j < len; ++j) {
+                    const uint32_t dd = d.pool_dist[base + j];
+                    if (dd >= iter) continue;
+                    const uint32_t hh = d.pool_hub[base + j];
+                    if (hh < rr && dd + (uint32_t)row[hh - bc.base] <= iter) { keep = false; break; }
+                }
+            }
+            if (keep) hs.offered[atomicAdd(&hs.ctr[3], 1u)] = idx;
+        }
+        __syncthreads();
+    }
+    const uint32_t nadd = hs.ctr[3];
+    if (nadd) {
+        // (d) reserve, relocating if the slot is too small
+        if (tid == 0) {
+            const uint32_t cap = d.lab_cap[t], need = len + nadd;
+            hs.ctr[5] = 1;
+            hs.ctr[6] = 0;
+            *hs.base = base;
+            if (need > cap) {
+                uint32_t ncap = max(max(2u * cap, need), 8u);
+                ncap = (ncap + 7u) & ~7u;
+                const unsigned long long pos = atomicAdd(d.pool_top, (unsigned long long)ncap);
+                if (pos + ncap > d.pool_cap) {
+                    hs.ctr[5] = 0;
+                } else {
+                    hs.ctr[6] = 1;
+                    hs.ctr[7] = ncap;
+                    *hs.base = pos;
+                }
+            }
+        }
+        __syncthreads();
+        if (!hs.ctr[5]) {
+            if (tid == 0) {
+                atomicOr(d.status, ST_POOL_RETRY);
+                a.retry[atomicAdd(a.retry_cnt, 1u)] = t;
+            }
+            return;  // uniform; nothing committed
+        }
+        const uint64_t nbase = *hs.base;
+        if (hs.ctr[6]) {
+            for (uint32_t j = tid; j < len; j += blockDim.x) {
+                d.pool_hub[nbase + j] = d.pool_hub[base + j];
+                d.pool_dist[nbase + j] = d.pool_dist[base + j];
+            }
+        }
+        const bool is_root = t >= s && t < bc.e;
+        for (uint32_t j = tid; j < nadd; j += blockDim.x) {
+            const uint32_t idx = hs.offered[j];
+            d.pool_hub[nbase + len + j] = s + idx;
+            d.pool_dist[nbase + len + j] = (uint8_t)iter;
+            if (is_root) bc.dm[(uint64_t)(t - s) * bc.dn + (s + idx - bc.base)] = (uint8_t)iter;
+            atomicMin(&hs.ctr[4], s + idx);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (hs.ctr[6]) {
+                d.lab_off[t] = nbase;
+                d.lab_cap[t] = hs.ctr[7];
+            }
+            d.lab_len[t] = len + nadd;
+            d.last_pos[cp][t] = nbase + len;
+            d.last_cnt[cp][t] = nadd;
+            d.last_min[cp][t] = hs.ctr[4];
+            d.act_stamp[cp][t] = a.lid_cur;
+            a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
+            if (a.gd_mut) atomicAdd(&a.gd_mut[bc.g].fcnt[cp], 1u);
+            bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0) + (hs.ctr[6] ? 10ull * len : 0);
+        }
+    }
+    for (uint32_t x = tid; x < d.words; x += blockDim.x) d.ind[(uint64_t)t * d.words + x] = hs.ind[x];
+    if (tid == 0) d.ind_stamp[t] = bc.b + 1;
+}
+
+// One light tail, processed by one warp.
+__device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, WarpRegion &wr,
+                                unsigned long long &bytes)
+{
+    const int lane = threadIdx.x & 31;
+    long long c0 = d.work ? clock64() : 0, c1 = 0;
+    // phase clock: adds the cycles since the last mark to slot `w` (profiling only)
+    auto tick = [&](int w) {
+        if (d.work) {
+            c1 = clock64();
+            if (lane == 0) atomicAdd(&d.work[w], (unsigned long long)(c1 - c0));
+            c0 = c1;
+        }
+    };
+    const BatchCtx bc = tail_ctx(d, a, t);
+    const uint32_t s = bc.s, iter = bc.iter;
+    const int pp = (a.lid_cur - 1) & 1, cp = a.lid_cur & 1;
+    const uint32_t lid_prev = a.lid_cur - 1;
+    bytes += 8 + 4ull * d.words;  // tail entry, indicator stamp and row
+    // (a) indicator row of t for this batch
+    const bool valid = d.ind_stamp[t] == bc.b + 1;
+    for (uint32_t x = lane; x < d.words; x += 32) wr.ind[x] = valid ? d.ind[(uint64_t)t * d.words + x] : 0u;
+    if (lane == 0) wr.ctr[0] = 0;
+    __syncwarp();
+    // (b) gather first offers from active neighbours (heads >= s)
+    const uint32_t e_end = d.off[t + 1];
+    for (uint32_t e0 = d.off[t]; e0 < e_end; e0 += 32) {
+        const uint32_t e = e0 + lane;
+        const bool in = e < e_end;
+        const uint32_t h = in ? d.adj[e] : 0u;
+        const bool ge = in && h >= s;
+        const bool act = ge && d.act_stamp[pp][h] == lid_prev;
+        uint32_t mask = __ballot_sync(FULL, act);
+        bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull;
+        while (mask) {
+            const int src = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const uint32_t hh = __shfl_sync(FULL, h, src);
+            const uint64_t pos = d.last_pos[pp][hh];
+            const uint32_t c = d.last_cnt[pp][hh];
+            bytes += 12 + 4ull * c;  // last-group position/count and its hubs
+            for (uint32_t j = lane; j < c; j += 32) {
+                const uint32_t r = d.pool_hub[pos + j];
+                if (r < t) {
+                    const uint32_t idx = r - s;
+                    const uint32_t bit = 1u << (idx & 31);
+                    const uint32_t old = atomicOr(&wr.ind[idx >> 5], bit);
+                    if (!(old & bit)) wr.offered[atomicAdd(&wr.ctr[0], 1u)] = (uint16_t)idx;
+                }
+            }
+        }
+        if (__ballot_sync(FULL, in && !ge)) break;
+    }
+    __syncwarp();
+    const uint32_t noff = wr.ctr[0];
+    tick(W_CYC_SCAN);
+    if (noff == 0) return;
+    bytes += 17ull * d.K + 4ull * d.words + 4;  // tail BP row; indicator write-back
+    // (c) BP test in two stages: lane per candidate on BP root 0 (which settles
+    // most pairs), then warp-cooperative over the remaining roots for the rest.
+    const ulonglong2 zero2 = make_ulonglong2(0, 0);
+    const uint8_t td0 = lane < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane] : (uint8_t)U8_INF;
+    const uint8_t td1 = lane + 32 < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane + 32] : (uint8_t)U8_INF;
+    const ulonglong2 ts0 = lane < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane] : zero2;
+    const ulonglong2 ts1 =
+        lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
+    const uint8_t tr0d = __shfl_sync(FULL, td0, 0);
+    const ulonglong2 tr0s = make_ulonglong2(__shfl_sync(FULL, ts0.x, 0), __shfl_sync(FULL, ts0.y, 0));
+    uint32_t nsurv = 0;
+    for (uint32_t c0 = 0; c0 < noff; c0 += 32) {
+        const uint32_t c = c0 + lane;
+        bool keep = false;
+        uint16_t idx = 0;
+        if (c < noff) {
+            idx = wr.offered[c];
+            const uint64_t rr = s + idx;
+            keep = d.K == 0 || !bp_one(d.bpd[rr * d.K], reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K], tr0d,
+                                       tr0s, iter);
+        }
+        const uint32_t km = __ballot_sync(FULL, keep);
+        __syncwarp();
+        if (keep) wr.offered[nsurv + __popc(km & ((1u << lane) - 1u))] = idx;
+        nsurv += __popc(km);
+        __syncwarp();
+    }
+    if (d.K > 1 && nsurv) {
+        uint32_t n2 = 0;
+        for (uint32_t c = 0; c < nsurv; c += 2) {
+            const uint16_t ia = wr.offered[c];
+            const bool two = c + 1 < nsurv;
+            const uint16_t ib = two ? wr.offered[c + 1] : ia;
+            const bool ca = bp_covered_warp(d, s + ia, lane, 1, td0, ts0, td1, ts1, iter);
+            const bool cb = two && bp_covered_warp(d, s + ib, lane, 1, td0, ts0, td1, ts1, iter);
+            __syncwarp();
+            if (lane == 0) {
+                if (!ca) wr.offered[n2] = ia;
+                if (two && !cb) wr.offered[n2 + (ca ? 0 : 1)] = ib;
+            }
+            n2 += (ca ? 0 : 1) + (two && !cb ? 1 : 0);
+            __syncwarp();
+        }
+        nsurv = n2;
+    }
+    tick(W_CYC_BP);
+    // (d) distance test against t's labels with d < iter
+    uint32_t nadd = 0;
+    const uint32_t len = d.lab_len[t];
+    uint64_t base = d.lab_off[t];
+    if (nsurv) {
+        if (lane == 0) wr.ctr[1] = 0;
+        __syncwarp();
+        for (uint32_t j = lane; j < len; j += 32) {
+            const uint8_t dd = d.pool_dist[base + j];
+            if (dd < iter) {
+                const uint32_t slot = atomicAdd(&wr.ctr[1], 1u);
+                if (slot < SMALL_CAP) {
+                    wr.sh[slot] = d.pool_hub[base + j];
+                    wr.sd[slot] = dd;
+                }
+            }
+        }
+        __syncwarp();
+        const uint32_t nsmall = wr.ctr[1];
+        bytes += 12 + (uint64_t)len + 4ull * min(nsmall, (uint32_t)SMALL_CAP) + (uint64_t)nsurv * nsmall;
+        for (uint32_t c0 = 0; c0 < nsurv; c0 += 32) {
+            const uint32_t c = c0 + lane;
+            bool keep = false;
+            uint16_t idx = 0;
+            if (c < nsurv) {
+                idx = wr.offered[c];
+                const uint32_t rr = s + idx;
+                const uint8_t *row = bc.dm + (uint64_t)idx * bc.dn;
+                keep = true;
+                if (nsmall <= SMALL_CAP) {
+                    for (uint32_t k = 0; k < nsmall; ++k) {
+                        const uint32_t hh = wr.sh[k];
+                        if (hh < rr && (uint32_t)wr.sd[k] + (uint32_t)row[hh - bc.base] <= iter) { keep = false; break; }
+                    }
+                } else {
+                    for (uint32_t j = 0; j < len; ++j) {
+                        const uint32_t dd = d.pool_dist[base + j];
+                        if (dd >= iter) continue;
+                        const uint32_t hh = d.pool_hub[base + j];
+                        if (hh < rr && dd + (uint32_t)row[hh - bc.base] <= iter) { keep = false; break; }
+                    }
+                }
+            }
+            const uint32_t km = __ballot_sync(FULL, keep);
+            __syncwarp();
+            if (keep) wr.offered[nadd + __popc(km & ((1u << lane) - 1u))] = idx;
+            nadd += __popc(km);
+            __syncwarp();
+        }
+    }
+    tick(W_CYC_DIST);
+    // (e) reserve room and commit
+    if (nadd) {
+        if (!warp_reserve(d, t, len + nadd, base, lane)) {
+            if (lane == 0) {
+                atomicOr(d.status, ST_POOL_RETRY);
+                a.retry[atomicAdd(a.retry_cnt, 1u)] = t;
+            }
+            return;  // nothing committed; re-run after the pool grows
+        }
+        const bool is_root = t >= s && t < bc.e;
+        uint32_t mn = 0xffffffffu;
+        for (uint32_t j = lane; j < nadd; j += 32) {
+            const uint32_t idx = wr.offered[j];
+            d.pool_hub[base + len + j] = s + idx;
+            d.pool_dist[base + len + j] = (uint8_t)iter;
+            if (is_root) bc.dm[(uint64_t)(t - s) * bc.dn + (s + idx - bc.base)] = (uint8_t)iter;
+            mn = min(mn, s + idx);
+        }
+        mn = warp_min_u32(mn);
+        bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0);
+        if (lane == 0) {
+            d.lab_len[t] = len + nadd;
+            d.last_pos[cp][t] = base + len;
+            d.last_cnt[cp][t] = nadd;
+            d.last_min[cp][t] = mn;
+            d.act_stamp[cp][t] = a.lid_cur;
+            a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
+            if (a.gd_mut) atomicAdd(&a.gd_mut[bc.g].fcnt[cp], 1u);
+        }
+    }
+    for (uint32_t x = lane; x < d.words; x += 32) d.ind[(uint64_t)t * d.words + x] = wr.ind[x];
+    if (lane == 0) d.ind_stamp[t] = bc.b + 1;
+    __syncwarp();
+    tick(W_CYC_COMMIT);
+}
+
+// Pull phase of a level: heavy tails block-by-block, then light tails
+// warp-by-warp.  Ends with the block converged.
+__device__ void pull_phase(const UnwDev &d, const PullArgs &a, unsigned char *pull_smem)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned long long bytes = 0;
+    const uint32_t hcnt = a.htails_cnt ? *a.htails_cnt : 0u;
+    if (hcnt) {
+        const long long h0 = d.work ? clock64() : 0;
+        HeavyRegion hs = heavy_region(pull_smem, d.words, d.B);
+        for (uint32_t q = blockIdx.x; q < hcnt; q += gridDim.x) {
+            pull_heavy_tail(d, a, a.htails[q], hs, bytes);
+            __syncthreads();
+        }
+        if (d.work && threadIdx.x == 0) atomicAdd(&d.work[W_CYC_HEAVY], (unsigned long long)(clock64() - h0));
+    }
+    const uint32_t cnt = *a.tails_cnt;
+    WarpRegion wr = warp_region(pull_smem, d.words, d.B, threadIdx.x >> 5);
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw)
+        pull_light_tail(d, a, a.tails[q], wr, bytes);
+    if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_PULL], bytes);
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Grid-wide barrier for persistent cooperative launches.  The spin is bounded:
+// after BARRIER_TIMEOUT_NS a block records ST_BARRIER_TIMEOUT and the barrier
+// returns false, so a logic error can never leave the GPU spinning.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long BARRIER_TIMEOUT_NS = 4000000000ull;
+constexpr uint32_t ST_BARRIER_TIMEOUT = 8u;
+
+struct GridBar {
+    uint32_t arrive, gen;
+};
+
+__device__ __forceinline__ uint32_t vload(const uint32_t *p) { return *(const volatile uint32_t *)p; }
+
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Returns false (in every thread of the block) if the wait timed out.
+__device__ bool grid_barrier(GridBar *bar, uint32_t *status)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile uint32_t *gen = &bar->gen;
+        const uint32_t g = *gen;
+        __threadfence();
+        const uint32_t arrived = atomicAdd(&bar->arrive, 1u) + 1u;
+        int good = 1;
+        if (arrived == gridDim.x) {
+            atomicExch(&bar->arrive, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            const unsigned long long t0 = gtimer();
+            while (*gen == g) {
+                __nanosleep(32);
+                if (gtimer() - t0 > BARRIER_TIMEOUT_NS) {
+                    atomicOr(status, ST_BARRIER_TIMEOUT);
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Final store: copy every list out of the pool, sorting each batch run by hub.
+// Runs are contiguous because batches append in order; the batch of hub h is
+// (h - base) / B, base = first id of the vertex's graph (0 for one graph, else
+// gbase[gmap[v]]), and hubs are stored graph-local (h - base).  Entries are
+// unique per vertex, so a rank-by-count sort is exact.
+__device__ void finalize_phase(const UnwDev &d, const uint64_t *fin_off, uint32_t *fin_hub, uint8_t *fin_dist,
+                               const uint16_t *gmap, const uint32_t *gbase)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < d.n; v += nw) {
+        const uint64_t base = d.lab_off[v], fo = fin_off[v];
+        const uint32_t len = d.lab_len[v];
+        const uint32_t gb = gmap ? gbase[gmap[v]] : 0u;
+        uint32_t rs = 0;
+        while (rs < len) {
+            const uint32_t batch = (d.pool_hub[base + rs] - gb) / d.B;
+            // run end: first entry of a later batch (monotone by batch)
+            uint32_t re = rs;
+            for (;;) {
+                const uint32_t j = re + lane;
+                const bool same = j < len && (d.pool_hub[base + j] - gb) / d.B == batch;
+                const uint32_t m = __ballot_sync(FULL, same);
+                if (m == FULL) { re += 32; continue; }
+                re += __ffs(~m) - 1;
+                break;
+            }
+            for (uint32_t c0 = rs; c0 < re; c0 += 32) {
+                const uint32_t j = c0 + lane;
+                const bool mine = j < re;
+                const uint32_t key = mine ? d.pool_hub[base + j] : 0xffffffffu;
+                const uint8_t dist = mine ? d.pool_dist[base + j] : 0;
+                uint32_t rank = 0;
+                for (uint32_t o0 = rs; o0 < re; o0 += 32) {
+                    const uint32_t oj = o0 + lane;
+                    const uint32_t other = oj < re ? d.pool_hub[base + oj] : 0xffffffffu;
+                    for (int k = 0; k < 32; ++k) rank += (__shfl_sync(FULL, other, k) < key) ? 1u : 0u;
+                }
+                if (mine) {
+                    fin_hub[fo + rs + rank] = key - gb;
+                    fin_dist[fo + rs + rank] = dist;
+                }
+            }
+            rs = re;
+        }
+    }
+}
+
+}  // namespace
+}  // namespace pado

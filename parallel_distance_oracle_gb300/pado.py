@@ -175,6 +175,141 @@ class VertexCentricPLL(_Index):
         return obj
 
 
+class _GraphArrays:
+    """Pointer arrays over many graphs for the many-graph entry points; keeps
+    the per-graph numpy arrays alive while the call runs."""
+
+    def __init__(self, graphs, ranks):
+        G = len(graphs)
+        if ranks is not None and len(ranks) != G:
+            raise ValueError("one rank array per graph")
+        self.G = G
+        self.n = np.array([g.n for g in graphs], np.uint32)
+        self._keep = []
+        self.off = (C.c_void_p * G)()
+        self.adj = (C.c_void_p * G)()
+        self.rank = (C.c_void_p * G)() if ranks is not None else None
+        for i, g in enumerate(graphs):
+            off, adj = _u64(g.off), _u32(g.adj)
+            self._keep += [off, adj]
+            self.off[i] = off.ctypes.data
+            self.adj[i] = adj.ctypes.data
+            if ranks is not None and ranks[i] is not None:
+                rk = _u32(ranks[i])
+                self._keep.append(rk)
+                self.rank[i] = rk.ctypes.data
+
+    def args(self):
+        return (self.G, ptr(self.n), C.cast(self.off, C.c_void_p), C.cast(self.adj, C.c_void_p),
+                C.cast(self.rank, C.c_void_p) if self.rank is not None else None)
+
+
+def build_many(graphs, ranks=None, bp_roots: int = 50, batch: int = 1024) -> list:
+    """Label many independent graphs together (pado_unw_build_many): returns
+    one VertexCentricPLL per graph, each with exactly the labels building it
+    alone gives."""
+    ga = _GraphArrays(graphs, ranks)
+    hs = (C.c_void_p * ga.G)()
+    check(lib.pado_unw_build_many(*ga.args(), bp_roots, batch, C.cast(hs, C.c_void_p)))
+    out = []
+    for i in range(ga.G):
+        idx = VertexCentricPLL(bp_roots=bp_roots, batch=batch)
+        idx._h = C.c_void_p(hs[i])
+        out.append(idx)
+    return out
+
+
+def tune_batch(graphs, ranks=None, bp_roots: int = 50, candidates=(256, 512, 1024, 2048), sample: int = 0):
+    """Pick the batch size for build_many by timing candidates on a sample of
+    the graphs (pado_unw_tune_batch).  Returns (best, {candidate: ms})."""
+    ga = _GraphArrays(graphs, ranks)
+    cand = _u32(candidates)
+    ms = np.zeros(len(cand), np.float32)
+    best = C.c_uint32()
+    check(lib.pado_unw_tune_batch(*ga.args(), bp_roots, ptr(cand), len(cand), sample, C.byref(best), ptr(ms)))
+    return int(best.value), {int(c): float(t) for c, t in zip(cand, ms)}
+
+
+_PADO_E_TIMEOUT = 6
+
+
+class Server:
+    """Serving loop over device-resident label sets (pado_server_*): requests of
+    any size from any thread are coalesced into mixed batches (continuous
+    batching); label sets are admitted and evicted by an HBM budget.  The
+    server borrows the indexes added to it until ``close()``."""
+
+    def __init__(self, hbm_budget_bytes: int, max_batch_pairs: int = 1 << 20, slots: int = 4):
+        h = C.c_void_p()
+        check(lib.pado_server_create(int(hbm_budget_bytes), max_batch_pairs, slots, C.byref(h)))
+        self._h = h
+        self._kinds = []
+        self._pending = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.pado_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, index: _Index) -> int:
+        i = C.c_uint32()
+        check(lib.pado_server_add(self._h, index._need(), C.byref(i)))
+        self._kinds.append(index.kind)
+        return int(i.value)
+
+    def submit(self, index_id: int, a, b) -> int:
+        """Queue a request; returns a ticket for ``wait``."""
+        a, b = _u32(a), _u32(b)
+        out = np.empty(a.shape, np.uint8 if self._kinds[index_id] == PADO_UNWEIGHTED else np.int16)
+        t = C.c_uint64()
+        check(lib.pado_server_submit(self._h, index_id, a.size, ptr(a), ptr(b), ptr(out), C.byref(t)))
+        self._pending[int(t.value)] = (a, b, out)
+        return int(t.value)
+
+    def wait(self, ticket: int, timeout_s: float = -1.0):
+        """Results of a submitted request and its latency in seconds."""
+        lat = C.c_double()
+        st = lib.pado_server_wait(self._h, ticket, timeout_s, C.byref(lat))
+        if st == _PADO_E_TIMEOUT:
+            check(st)  # still outstanding: keep its buffers
+        a, b, out = self._pending.pop(ticket)
+        check(st)
+        return out, float(lat.value)
+
+    def query(self, index_id: int, a, b):
+        return self.wait(self.submit(index_id, a, b))[0]
+
+    def stats(self) -> dict:
+        s = _lib.ServerStats()
+        check(lib.pado_server_get_stats(self._h, C.byref(s)))
+        return {f: int(getattr(s, f)) for f, _ in s._fields_ if f != "pad"}
+
+    def replay(self, arrival_s, index_id, k, a, b, mode: int = 0):
+        """Open-loop replay of a request trace (pado_server_replay).  Returns
+        (out8, out16, latency_s); request i's results are out8/out16
+        [pair_off[i]: pair_off[i] + k[i]] with pair_off the prefix sum of k."""
+        arrival_s = np.ascontiguousarray(arrival_s, np.float64)
+        index_id = _u32(index_id)
+        k = _u64(k)
+        pair_off = np.zeros(len(k), np.uint64)
+        if len(k) > 1:
+            np.cumsum(k[:-1], out=pair_off[1:])
+        a, b = _u32(a), _u32(b)
+        total = int(k.sum())
+        out8 = np.zeros(max(total, 1), np.uint8)
+        out16 = np.zeros(max(total, 1), np.int16)
+        lat = np.zeros(len(k), np.float64)
+        check(lib.pado_server_replay(self._h, len(k), ptr(arrival_s), ptr(index_id), ptr(k), ptr(pair_off), ptr(a),
+                                     ptr(b), ptr(out8), ptr(out16), mode, ptr(lat)))
+        return out8[:total], out16[:total], lat
+
+
 # The OpenMP class of the reference computes the same labels
 # (pado_unw_unv_para.201912311607.parallel_bp_labeling.h:42-304).
 ParaVertexCentricPLL = VertexCentricPLL
