@@ -35,16 +35,16 @@ from parallel_distance_oracle_gb300 import graphs as G  # noqa: E402
 
 WORKLOADS = {
     # unweighted social-like R-MAT s20/ef16, 64 BP roots, batch 1024, 10M queries
-    "rmat20": dict(kind="unw", scale=20, ef=16, seed=2, K=64, B=1024, queries=10_000_000, qseed=12,
+    "rmat20": dict(kind="unw", scale=20, ef=16, seed=2, K=64, B=1024, queries=10_000_000, qseed=12, ref_batches=12,
                    desc="R-MAT s20 ef16 (a,b,c=.57,.19,.19), dedup+symmetrised, degree order, K=64, B=1024"),
     # R-MAT s14/ef8, K=50: the case a CPU labels in under a second
-    "rmat14": dict(kind="unw", scale=14, ef=8, seed=1, K=50, B=1024, queries=100_000, qseed=11,
+    "rmat14": dict(kind="unw", scale=14, ef=8, seed=1, K=50, B=1024, queries=100_000, qseed=11, ref_batches=16,
                    desc="R-MAT s14 ef8, degree order, K=50, B=1024"),
     # a smaller case of the same kernels, sized for ncu captures (a few GB on the device)
-    "rmat18": dict(kind="unw", scale=18, ef=16, seed=2, K=64, B=1024, queries=1_000_000, qseed=12,
+    "rmat18": dict(kind="unw", scale=18, ef=16, seed=2, K=64, B=1024, queries=1_000_000, qseed=12, ref_batches=12,
                    desc="R-MAT s18 ef16, degree order, K=64, B=1024 (profiling case)"),
     # weighted R-MAT s18/ef8, weights 1..100, batch 512
-    "wrmat18": dict(kind="w", scale=18, ef=8, seed=3, K=0, B=512, queries=1_000_000, qseed=13,
+    "wrmat18": dict(kind="w", scale=18, ef=8, seed=3, K=0, B=512, queries=1_000_000, qseed=13, ref_batches=0,
                     desc="weighted R-MAT s18 ef8, weights U[1,100], degree order, B=512"),
 }
 # Many independent graphs labeled together: 512 graphs, n log-uniform in
@@ -58,8 +58,8 @@ MANY = dict(graphs=512, n_lo=1000, n_hi=20000, er_degree=6, grid_frac=0.02, K=64
 # workload's graphs in HBM under a 40 GB admission budget; open-loop Poisson
 # arrivals; each request asks one label set (uniform) for k pairs, k
 # log-uniform in [1, 65536], endpoints Zipf(1.1) over degree rank.
-SERVE = dict(budget=40 << 30, graphs=64, kmax=65536, zipf=1.1, rates=(1e4, 3e4, 1e5, 3e5, 1e6, 1e7),
-             pairs_per_rate=40_000_000, max_batch_pairs=1 << 20, slots=4, seed=9)
+SERVE = dict(budget=40 << 30, graphs=64, kmax=65536, zipf=1.1, rates=(1e4, 3e4, 5e4, 1e5, 3e5, 1e6, 1e7),
+             pairs_per_rate=40_000_000, max_batch_pairs=1 << 18, slots=8, seed=9)
 METRIC = "labels_per_s"
 UNIT = "labels/s"
 
@@ -213,7 +213,8 @@ def main():
     ap.add_argument("--many-batch", type=int, default=0, help="skip tuning and use this batch size")
     ap.add_argument("--queries", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-batches", type=int, default=1, help="root batches in one CPU-baseline sample")
+    ap.add_argument("--ref-batches", type=int, default=None,
+                    help="root batches in one CPU-baseline sample (default: per workload)")
     ap.add_argument("--no-profile", action="store_true")
     args = ap.parse_args()
     if args.workload == "many":
@@ -221,6 +222,8 @@ def main():
     if args.workload == "serve":
         return run_serve(args)
     wl = WORKLOADS[args.workload]
+    if args.ref_batches is None:
+        args.ref_batches = wl["ref_batches"]
     if args.impl == "reference":
         return run_reference(args, wl)
 
@@ -349,14 +352,9 @@ def main():
         pidx.order_labels(rank=rk)
         pidx.query_device(da.data_ptr(), db.data_ptr(), dout.data_ptr(), nq, stream.cuda_stream)
         torch.cuda.synchronize()
-        need = lib.pado_profile_read(None, 0, 0)
-        buf = C.create_string_buffer(need + 16)
-        lib.pado_profile_read(buf, len(buf), 1)
+        prof = read_profile(lib)
         _lib.check(lib.pado_profile(0))
         pidx.close()
-        for ln in buf.value.decode().splitlines():
-            name, launches_k, ms, byts = ln.split()
-            prof[name] = {"launches": int(launches_k), "ms": float(ms), "bytes": int(byts)}
     # the persistent loop kernel runs the mark and pull phases: its algorithmic
     # bytes are those two counters
     if "label_loop_kernel" in prof:
@@ -502,6 +500,14 @@ def run_many(args):
     one_wall = time.perf_counter() - t0
     one_launches = lib.pado_kernel_launches() - l0
     assert one_counts == counts, "batched and one-at-a-time label counts differ"
+    prof = {}
+    if not args.no_profile:
+        _lib.check(lib.pado_profile(1))
+        for ix in pado.build_many(gs, ranks, bp_roots=K, batch=B):
+            ix.close()
+        torch.cuda.synchronize()
+        prof = read_profile(lib)
+        _lib.check(lib.pado_profile(0))
     dev_mean, wall_mean = statistics.mean(dev_s), statistics.mean(wall_s)
     out = {
         "metric": METRIC, "value": labels / dev_mean, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
@@ -518,9 +524,22 @@ def run_many(args):
         "e2e": {"value": labels / wall_mean, "unit": UNIT,
                 "h2d_bytes_per_step": int(sum(g.off.nbytes + g.adj.nbytes for g in gs)),
                 "d2h_bytes_per_step": 0, "note": "host CSR arrays in, device-resident indexes out"},
-        "clocks": clocks, "gpu_launches": launches,
+        "clocks": clocks, "gpu_launches": launches, "profile": prof,
     }
     print(json.dumps(out), flush=True)
+
+
+def read_profile(lib):
+    """Per-kernel launches, device ms and algorithmic bytes of the profiled
+    calls (pado_profile_read), reset after reading."""
+    need = lib.pado_profile_read(None, 0, 0)
+    buf = C.create_string_buffer(need + 16)
+    lib.pado_profile_read(buf, len(buf), 1)
+    prof = {}
+    for ln in buf.value.decode().splitlines():
+        name, launches_k, ms, byts = ln.split()
+        prof[name] = {"launches": int(launches_k), "ms": float(ms), "bytes": int(byts)}
+    return prof
 
 
 def run_serve(args):
@@ -633,15 +652,21 @@ def run_serve(args):
 
 
 def traffic_from_profiles(kernel: str, workload: str):
-    """DRAM bytes per launch for `kernel` from the committed ncu summary
-    (profiles/ncu_traffic.json: {"<workload>:<kernel>": bytes_per_launch})."""
-    p = REPO / "profiles" / "ncu_traffic.json"
+    """DRAM bytes per launch of `kernel` on `workload` (dram__bytes_read.sum +
+    dram__bytes_write.sum from one ncu capture), read from the table in the
+    committed summary profiles/dram_traffic.md:
+    | workload | kernel | dram bytes per launch | how |"""
+    p = REPO / "profiles" / "dram_traffic.md"
     if not p.exists():
         return None
-    try:
-        return json.loads(p.read_text()).get(f"{workload}:{kernel}")
-    except Exception:
-        return None
+    for ln in p.read_text().splitlines():
+        cells = [c.strip() for c in ln.strip().strip("|").split("|")]
+        if len(cells) >= 3 and cells[0] == workload and cells[1] == kernel:
+            try:
+                return float(cells[2].replace(",", ""))
+            except ValueError:
+                return None
+    return None
 
 
 if __name__ == "__main__":

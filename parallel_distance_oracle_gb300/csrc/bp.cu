@@ -14,15 +14,23 @@
 //   * stored row: (d, S^-1, S^0 & ~S^-1) (:377-381); an unused slot (no root
 //     left) stores d = 255 and empty sets (:288-292).
 // Device mapping: the BFS of up to GROUP roots run together, level by level,
-// over one combined frontier of (slot, vertex) entries.  Per level, kernel 1
-// lets each frontier vertex pull S^0 from its same-level neighbours (64-bit OR
-// reduction), kernel 2 pushes along child edges, claiming undiscovered vertices
-// with a CAS on a 32-bit level array and ORing the sets with 64-bit atomicOr.
-// Frontier vertices of degree >= HEAVY are spread over every warp of the grid
-// (each warp takes 32-edge chunks and ORs its share atomically); lighter ones
-// get one warp each.  OR is order-independent, so rows are bit-identical.
-// Per root the adjacency of every reached vertex is streamed twice (sibling and
-// child kernels) with a 4 B level lookup per edge; per-vertex state is 20 B.
+// over one combined frontier of (slot, vertex) entries, and every set update
+// is a PULL (an OR reduction over a vertex's own adjacency, stored by the one
+// thread that owns the vertex) instead of a per-edge atomic push:
+//   bp_level_kernel(d):  each v at level d ORs S^-1 of its level-d neighbours
+//       into S^0[v] (the sibling step) and claims its unreached neighbours for
+//       level d+1 (CAS on the level array; warp-aggregated appends);
+//   bp_parent_kernel(d): each u at level d+1 ORs S^-1 and S^0 of its level-d
+//       neighbours (its parents, whose S^0 the previous kernel finished) into
+//       its own sets (the child step).
+// The child step of the reference pushes parent sets along every d -> d+1
+// edge; pulling them over the same edges gives the same ORs.  Frontier
+// vertices of degree >= HEAVY are spread over every warp of the grid (partial
+// ORs combined with one atomicOr per warp); those of degree <= SMALL_DEG get
+// SUB lanes each (8 per warp: most vertices of sparse graphs); the rest get one
+// warp each.  OR is order-independent, so rows are bit-identical.  Per root
+// the adjacency of every reached vertex is streamed twice with a 4 B level
+// lookup per edge; per-vertex state is 20 B.
 
 #include <algorithm>
 
@@ -34,6 +42,15 @@ namespace {
 constexpr uint32_t LV_INF = 255u;
 constexpr uint32_t GROUP = 16;       // BP roots labeled concurrently
 constexpr uint32_t HEAVY = 4096;     // frontier vertices split over all warps
+constexpr uint32_t SMALL_DEG = 16;   // frontier vertices up to this degree share a warp ...
+constexpr uint32_t SUB = 4;          // ... SUB lanes each
+
+enum FrontClass : int { FC_LIGHT = 0, FC_HEAVY = 1, FC_SMALL = 2 };
+
+__host__ __device__ __forceinline__ int front_class(uint32_t deg)
+{
+    return deg >= HEAVY ? FC_HEAVY : (deg <= SMALL_DEG ? FC_SMALL : FC_LIGHT);
+}
 
 __device__ __forceinline__ uint64_t warp_or64(uint64_t v)
 {
@@ -57,11 +74,14 @@ struct BpState {
 __device__ __forceinline__ uint32_t ent_slot(uint64_t e) { return (uint32_t)(e >> 32); }
 __device__ __forceinline__ uint32_t ent_v(uint64_t e) { return (uint32_t)e; }
 
+// A frontier: entry lists by class (FC_*), with their counts.
 struct Front {
-    const uint64_t *light;
-    const uint32_t *light_cnt;
-    const uint64_t *heavy;
-    const uint32_t *heavy_cnt;
+    const uint64_t *list[3];
+    const uint32_t *cnt;  // cnt[FC_*]
+};
+struct NextFront {
+    uint64_t *list[3];
+    uint32_t *cnt;
 };
 
 __global__ void bp_reset_kernel(BpState st)
@@ -86,113 +106,136 @@ __global__ void bp_seed_kernel(BpState st, const uint32_t *sslot, const uint32_t
     }
 }
 
-// Sibling step of level d: S^0[v] |= S^-1[tv] for tv adjacent at the same level.
-__global__ void __launch_bounds__(256, 4) bp_sibling_kernel(BpState st, Front f, uint32_t d)
+// Per-entry accumulator of the two pull kernels.
+struct BpAcc {
+    uint64_t a = 0, b = 0;
+    uint32_t hits = 0;
+};
+
+// Runs `edge(so, slot, v, tv, acc)` over the adjacency of every frontier entry
+// and `fin(so, v, acc, atomic)` once per entry with the entry's OR-reduced
+// accumulator (atomic: several warps share the entry, combine with atomicOr).
+template <class Edge, class Fin>
+__device__ __forceinline__ void bp_pull(const BpState &st, const Front &f, unsigned long long &bytes, Edge edge, Fin fin)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    unsigned long long bytes = 0;
     // heavy vertices: every warp takes 32-edge chunks of each
-    const uint32_t hc = *f.heavy_cnt;
+    const uint32_t hc = f.cnt[FC_HEAVY];
     for (uint32_t q = 0; q < hc; ++q) {
-        const uint64_t ent = f.heavy[q];
+        const uint64_t ent = f.list[FC_HEAVY][q];
         const uint32_t slot = ent_slot(ent), v = ent_v(ent);
         const uint64_t so = (uint64_t)slot * st.n;
         const uint32_t e_end = st.off[v + 1];
-        uint64_t acc = 0;
-        uint32_t same = 0;
-        for (uint32_t e = st.off[v] + gw * 32 + lane; e < e_end; e += nw * 32) {
-            const uint32_t tv = st.adj[e];
-            if (st.lvl[so + tv] == d) {
-                acc |= st.sm1[so + tv];
-                ++same;
-            }
-        }
-        acc = warp_or64(acc);
-        if (lane == 0 && acc) atomicOr((unsigned long long *)&st.s0[so + v], (unsigned long long)acc);
+        BpAcc acc;
+        for (uint32_t e = st.off[v] + gw * 32 + lane; e < e_end; e += nw * 32) edge(so, slot, v, st.adj[e], acc);
+        acc.a = warp_or64(acc.a);
+        acc.b = warp_or64(acc.b);
+        if (lane == 0) fin(so, v, acc, true);
         if (lane == 0 && gw == 0) bytes += 20 + 8ull * (e_end - st.off[v]);
-        bytes += 8ull * same;
+        bytes += 8ull * acc.hits;
     }
-    const uint32_t lc = *f.light_cnt;
+    // light vertices: a warp each
+    const uint32_t lc = f.cnt[FC_LIGHT];
     for (uint32_t q = gw; q < lc; q += nw) {
-        const uint64_t ent = f.light[q];
+        const uint64_t ent = f.list[FC_LIGHT][q];
         const uint32_t slot = ent_slot(ent), v = ent_v(ent);
         const uint64_t so = (uint64_t)slot * st.n;
-        uint64_t acc = 0;
-        uint32_t same = 0;
-        for (uint32_t e = st.off[v] + lane; e < st.off[v + 1]; e += 32) {
-            const uint32_t tv = st.adj[e];
-            if (st.lvl[so + tv] == d) {
-                acc |= st.sm1[so + tv];
-                ++same;
-            }
+        const uint32_t e_end = st.off[v + 1];
+        BpAcc acc;
+        for (uint32_t e = st.off[v] + lane; e < e_end; e += 32) edge(so, slot, v, st.adj[e], acc);
+        acc.a = warp_or64(acc.a);
+        acc.b = warp_or64(acc.b);
+        if (lane == 0) {
+            fin(so, v, acc, false);
+            bytes += 20 + 8ull * (e_end - st.off[v]);
         }
-        acc = warp_or64(acc);
-        if (lane == 0 && acc) st.s0[so + v] |= acc;
-        if (lane == 0) bytes += 20 + 8ull * (st.off[v + 1] - st.off[v]);
-        bytes += 8ull * same;
+        bytes += 8ull * acc.hits;
     }
+    // small vertices: SUB lanes each, 32 / SUB per warp (warp-uniform loop)
+    const uint32_t sc = f.cnt[FC_SMALL];
+    const uint32_t per = 32 / SUB, sub = lane % SUB;
+    for (uint64_t qb = (uint64_t)gw * per; qb < sc; qb += (uint64_t)nw * per) {
+        const uint64_t q = qb + lane / SUB;
+        BpAcc acc;
+        uint64_t so = 0;
+        uint32_t v = 0;
+        if (q < sc) {
+            const uint64_t ent = f.list[FC_SMALL][q];
+            const uint32_t slot = ent_slot(ent);
+            v = ent_v(ent);
+            so = (uint64_t)slot * st.n;
+            const uint32_t e_end = st.off[v + 1];
+            for (uint32_t e = st.off[v] + sub; e < e_end; e += SUB) edge(so, slot, v, st.adj[e], acc);
+            if (sub == 0) bytes += 20 + 8ull * (e_end - st.off[v]);
+        }
+#pragma unroll
+        for (int o = 1; o < (int)SUB; o <<= 1) {
+            acc.a |= __shfl_xor_sync(0xffffffffu, acc.a, o);
+            acc.b |= __shfl_xor_sync(0xffffffffu, acc.b, o);
+        }
+        if (q < sc && sub == 0) fin(so, v, acc, false);
+        bytes += 8ull * acc.hits;
+    }
+}
+
+// Level d: the sibling step (S^0[v] |= S^-1[tv], tv at level d) and the
+// discovery of level d+1 (pado_unw_unv_unp.h:362-371).
+__global__ void __launch_bounds__(256, 4) bp_level_kernel(BpState st, Front f, uint32_t d, NextFront nx,
+                                                          uint32_t *status)
+{
+    unsigned long long bytes = 0;
+    bp_pull(
+        st, f, bytes,
+        [&](uint64_t so, uint32_t slot, uint32_t, uint32_t tv, BpAcc &acc) {
+            const uint32_t l = st.lvl[so + tv];
+            if (l == d) {
+                acc.a |= st.sm1[so + tv];
+                ++acc.hits;
+            } else if (l == LV_INF) {
+                if (d + 1 >= LV_INF) {
+                    atomicOr(status, ST_LEVEL_OVERFLOW);
+                } else if (atomicCAS(&st.lvl[so + tv], LV_INF, d + 1) == LV_INF) {
+                    const int c = front_class(st.off[tv + 1] - st.off[tv]);
+                    nx.list[c][agg_append_by(&nx.cnt[c], (unsigned)c)] = ((uint64_t)slot << 32) | tv;
+                    acc.hits += 2;
+                }
+            }
+        },
+        [&](uint64_t so, uint32_t v, const BpAcc &acc, bool atomic) {
+            if (!acc.a) return;
+            if (atomic)
+                atomicOr((unsigned long long *)&st.s0[so + v], (unsigned long long)acc.a);
+            else
+                st.s0[so + v] |= acc.a;
+        });
     if (st.work && bytes) atomicAdd(&st.work[W_BP_SIB], bytes);
 }
 
-__device__ __forceinline__ void bp_child_edge(const BpState &st, uint64_t so, uint32_t slot, uint32_t tv, uint32_t d,
-                                              uint64_t a, uint64_t b, uint64_t *next_l, uint32_t *next_l_cnt,
-                                              uint64_t *next_h, uint32_t *next_h_cnt, uint32_t *status,
-                                              unsigned long long &bytes)
+// The child step for the vertices first reached at level d+1: OR the sets of
+// their level-d neighbours (pado_unw_unv_unp.h:367-371).
+__global__ void __launch_bounds__(256, 4) bp_parent_kernel(BpState st, Front f, uint32_t d)
 {
-    const uint32_t t = st.lvl[so + tv];
-    if (t <= d) return;
-    if (t == LV_INF) {
-        if (d + 1 >= LV_INF) {
-            atomicOr(status, ST_LEVEL_OVERFLOW);
-            return;
-        }
-        if (atomicCAS(&st.lvl[so + tv], LV_INF, d + 1) == LV_INF) {
-            const uint64_t ent = ((uint64_t)slot << 32) | tv;
-            if (st.off[tv + 1] - st.off[tv] >= HEAVY)
-                next_h[atomicAdd(next_h_cnt, 1u)] = ent;
-            else
-                next_l[atomicAdd(next_l_cnt, 1u)] = ent;
-            bytes += 16;
-        }
-    }
-    if (a) atomicOr((unsigned long long *)&st.sm1[so + tv], (unsigned long long)a);
-    if (b) atomicOr((unsigned long long *)&st.s0[so + tv], (unsigned long long)b);
-    bytes += 16;
-}
-
-// Child step of level d: claim unreached neighbours for level d+1 and OR the
-// parent's sets into every level-(d+1) neighbour.
-__global__ void __launch_bounds__(256, 4) bp_child_kernel(BpState st, Front f, uint32_t d, uint64_t *next_l,
-                                                       uint32_t *next_l_cnt, uint64_t *next_h, uint32_t *next_h_cnt,
-                                                       uint32_t *status)
-{
-    const int lane = threadIdx.x & 31;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     unsigned long long bytes = 0;
-    const uint32_t hc = *f.heavy_cnt;
-    for (uint32_t q = 0; q < hc; ++q) {
-        const uint64_t ent = f.heavy[q];
-        const uint32_t slot = ent_slot(ent), v = ent_v(ent);
-        const uint64_t so = (uint64_t)slot * st.n;
-        const uint64_t a = st.sm1[so + v], b = st.s0[so + v];
-        const uint32_t e_end = st.off[v + 1];
-        if (lane == 0 && gw == 0) bytes += 28 + 8ull * (e_end - st.off[v]);
-        for (uint32_t e = st.off[v] + gw * 32 + lane; e < e_end; e += nw * 32)
-            bp_child_edge(st, so, slot, st.adj[e], d, a, b, next_l, next_l_cnt, next_h, next_h_cnt, status, bytes);
-    }
-    const uint32_t lc = *f.light_cnt;
-    for (uint32_t q = gw; q < lc; q += nw) {
-        const uint64_t ent = f.light[q];
-        const uint32_t slot = ent_slot(ent), v = ent_v(ent);
-        const uint64_t so = (uint64_t)slot * st.n;
-        const uint64_t a = st.sm1[so + v], b = st.s0[so + v];
-        if (lane == 0) bytes += 28 + 8ull * (st.off[v + 1] - st.off[v]);
-        for (uint32_t e = st.off[v] + lane; e < st.off[v + 1]; e += 32)
-            bp_child_edge(st, so, slot, st.adj[e], d, a, b, next_l, next_l_cnt, next_h, next_h_cnt, status, bytes);
-    }
+    bp_pull(
+        st, f, bytes,
+        [&](uint64_t so, uint32_t, uint32_t, uint32_t p, BpAcc &acc) {
+            if (st.lvl[so + p] == d) {
+                acc.a |= st.sm1[so + p];
+                acc.b |= st.s0[so + p];
+                acc.hits += 2;
+            }
+        },
+        [&](uint64_t so, uint32_t u, const BpAcc &acc, bool atomic) {
+            if (atomic) {
+                if (acc.a) atomicOr((unsigned long long *)&st.sm1[so + u], (unsigned long long)acc.a);
+                if (acc.b) atomicOr((unsigned long long *)&st.s0[so + u], (unsigned long long)acc.b);
+            } else {
+                if (acc.a) st.sm1[so + u] |= acc.a;
+                if (acc.b) st.s0[so + u] |= acc.b;
+            }
+        });
     if (st.work && bytes) atomicAdd(&st.work[W_BP_CHILD], bytes);
 }
 
@@ -271,8 +314,10 @@ BpResult bp_run(const HostGraph &hg, const DevGraph &g, uint32_t K, const std::v
     const uint32_t gsize = std::min<uint32_t>(GROUP, std::max<uint32_t>(nroots, 1));
     DBuf<uint32_t> lvl((uint64_t)gsize * n), cnts(8), status(1);
     DBuf<uint64_t> sm1((uint64_t)gsize * n), s0((uint64_t)gsize * n);
-    DBuf<uint64_t> fl0((uint64_t)gsize * n), fl1((uint64_t)gsize * n), fh0((uint64_t)gsize * n),
-        fh1((uint64_t)gsize * n);
+    // frontier lists by class, double-buffered: fr[buffer][class]
+    DBuf<uint64_t> fr[2][3];
+    for (auto &side : fr)
+        for (auto &l : side) l.alloc((uint64_t)gsize * n);
     size_t max_seeds = 1;
     for (uint32_t i = 0; i < nroots; i += gsize) {
         size_t c = 0;
@@ -296,7 +341,7 @@ BpResult bp_run(const HostGraph &hg, const DevGraph &g, uint32_t K, const std::v
             BpState st{n, slots, g.off.p, g.adj.p, lvl.p, sm1.p, s0.p, work_counters()};
             PADO_LAUNCH("bp_reset_kernel", s, bp_reset_kernel<<<grid_for((uint64_t)slots * n, vb), vb, 0, s>>>(st));
             std::vector<uint32_t> ss, sv, sl;
-            std::vector<uint64_t> sb, f0l, f0h, f1l, f1h;
+            std::vector<uint64_t> sb, f0[3], f1[3];
             for (uint32_t j = 0; j < slots; ++j) {
                 for (const BpSeed &x : seeds[g0 + j]) {
                     ss.push_back(j);
@@ -304,11 +349,8 @@ BpResult bp_run(const HostGraph &hg, const DevGraph &g, uint32_t K, const std::v
                     sl.push_back(x.lvl);
                     sb.push_back(x.bits);
                     const uint64_t ent = ((uint64_t)j << 32) | x.v;
-                    const bool heavy = hg.off[x.v + 1] - hg.off[x.v] >= HEAVY;
-                    if (x.lvl == 0)
-                        (heavy ? f0h : f0l).push_back(ent);
-                    else
-                        (heavy ? f1h : f1l).push_back(ent);
+                    const int c = front_class(hg.off[x.v + 1] - hg.off[x.v]);
+                    (x.lvl == 0 ? f0 : f1)[c].push_back(ent);
                 }
             }
             seed_slot.upload(ss.data(), ss.size(), s);
@@ -319,32 +361,34 @@ BpResult bp_run(const HostGraph &hg, const DevGraph &g, uint32_t K, const std::v
                         bp_seed_kernel<<<grid_for(sv.size(), 128), 128, 0, s>>>(st, seed_slot.p, seed_v.p, seed_l.p,
                                                                               seed_b.p, (uint32_t)sv.size()));
             // frontier 0 = the roots; frontier 1 starts with the selected neighbours
-            uint64_t *cur_l = fl0.p, *cur_h = fh0.p, *nxt_l = fl1.p, *nxt_h = fh1.p;
-            fl0.upload(f0l.data(), f0l.size(), s);
-            fh0.upload(f0h.data(), f0h.size(), s);
-            fl1.upload(f1l.data(), f1l.size(), s);
-            fh1.upload(f1h.data(), f1h.size(), s);
-            uint32_t init_cnt[4] = {(uint32_t)f0l.size(), (uint32_t)f0h.size(), (uint32_t)f1l.size(),
-                                    (uint32_t)f1h.size()};
+            uint32_t init_cnt[8] = {};
+            for (int c = 0; c < 3; ++c) {
+                fr[0][c].upload(f0[c].data(), f0[c].size(), s);
+                fr[1][c].upload(f1[c].data(), f1[c].size(), s);
+                init_cnt[c] = (uint32_t)f0[c].size();
+                init_cnt[4 + c] = (uint32_t)f1[c].size();
+            }
             PADO_CUDA(cudaMemcpyAsync(cnts.p, init_cnt, sizeof(init_cnt), cudaMemcpyHostToDevice, s));
-            uint32_t *cc = cnts.p, *nc = cnts.p + 2;  // [light, heavy] counts of current / next
-            uint32_t fsize = (uint32_t)(f0l.size() + f0h.size());
+            int cur = 0;  // fr[cur] / counts cnts[4*cur ..] hold level d
+            uint32_t fsize = (uint32_t)(f0[0].size() + f0[1].size() + f0[2].size());
             for (uint32_t d = 0; fsize > 0; ++d) {
-                Front f{cur_l, cc, cur_h, cc + 1};
-                PADO_LAUNCH("bp_sibling_kernel", s, bp_sibling_kernel<<<level_grid, 256, 0, s>>>(st, f, d));
-                PADO_LAUNCH("bp_child_kernel", s,
-                            bp_child_kernel<<<level_grid, 256, 0, s>>>(st, f, d, nxt_l, nc, nxt_h, nc + 1, status.p));
+                uint32_t *cc = cnts.p + 4 * cur, *nc = cnts.p + 4 * (cur ^ 1);
+                Front f{{fr[cur][0].p, fr[cur][1].p, fr[cur][2].p}, cc};
+                NextFront nx{{fr[cur ^ 1][0].p, fr[cur ^ 1][1].p, fr[cur ^ 1][2].p}, nc};
+                PADO_LAUNCH("bp_level_kernel", s,
+                            bp_level_kernel<<<level_grid, 256, 0, s>>>(st, f, d, nx, status.p));
+                // the next frontier, complete now, pulls its parents' sets
+                const Front fn{{nx.list[0], nx.list[1], nx.list[2]}, nc};
+                PADO_LAUNCH("bp_parent_kernel", s, bp_parent_kernel<<<level_grid, 256, 0, s>>>(st, fn, d));
                 ++res.levels;
-                PADO_CUDA(cudaMemcpyAsync(h_cnt, nc, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-                PADO_CUDA(cudaMemcpyAsync(h_cnt + 2, status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-                PADO_CUDA(cudaMemsetAsync(cc, 0, 2 * sizeof(uint32_t), s));
+                PADO_CUDA(cudaMemcpyAsync(h_cnt, nc, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+                PADO_CUDA(cudaMemcpyAsync(h_cnt + 3, status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+                PADO_CUDA(cudaMemsetAsync(cc, 0, 3 * sizeof(uint32_t), s));
                 PADO_CUDA(cudaStreamSynchronize(s));
-                if (h_cnt[2] & ST_LEVEL_OVERFLOW)
+                if (h_cnt[3] & ST_LEVEL_OVERFLOW)
                     throw Error(PADO_E_OVERFLOW, "bit-parallel BFS reached level 255 (uint8 distance overflow)");
-                fsize = h_cnt[0] + h_cnt[1];
-                std::swap(cur_l, nxt_l);
-                std::swap(cur_h, nxt_h);
-                std::swap(cc, nc);
+                fsize = h_cnt[0] + h_cnt[1] + h_cnt[2];
+                cur ^= 1;
             }
             PADO_LAUNCH("bp_store_kernel", s,
                         bp_store_kernel<<<grid_for(n, vb), vb, 0, s>>>(st, K, g0, d_bpd, d_bps));

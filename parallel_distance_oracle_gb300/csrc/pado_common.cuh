@@ -1,6 +1,7 @@
 // pado_common.cuh -- shared device/host helpers for the PADO GPU library.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -120,6 +121,31 @@ inline unsigned grid_for(uint64_t items, unsigned block, unsigned cap = 152u * 6
     return (unsigned)g;
 }
 
+#ifdef __CUDACC__
+// Slot for one new entry of a list whose length is *cnt.  The threads that
+// reach this call together share one atomicAdd (warp-aggregated), which keeps
+// a global list counter from serialising every append of a wide frontier.
+__device__ __forceinline__ uint32_t agg_append(uint32_t *cnt)
+{
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(cnt, (uint32_t)g.size());
+    return g.shfl(base, 0) + g.thread_rank();
+}
+
+// Same, for threads that may target different counters: they are grouped by
+// the counter's class `c` first.
+__device__ __forceinline__ uint32_t agg_append_by(uint32_t *cnt, unsigned c)
+{
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::labeled_partition(cg::coalesced_threads(), c);
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(cnt, (uint32_t)g.size());
+    return g.shfl(base, 0) + g.thread_rank();
+}
+#endif
+
 // Device-side status word bits (written by kernels, read by the host).
 enum : uint32_t {
     ST_LEVEL_OVERFLOW = 1u,   // a BFS level reached 255 (uint8 distance)
@@ -159,10 +185,13 @@ inline uint64_t debug_pool_entries()
     const char *e = std::getenv("PADO_DEBUG_POOL_ENTRIES");
     return e ? std::strtoull(e, nullptr, 10) : 0;
 }
+// The label pool starts at 160 entries per vertex (0.8 KB/vertex unweighted,
+// capped at 2^31 entries): enough for a social-graph labeling plus its list
+// relocations in one persistent launch, so growth relaunches are rare.
 inline uint64_t initial_pool_entries(uint32_t n)
 {
     const uint64_t dbg = debug_pool_entries();
-    return dbg ? dbg : std::max<uint64_t>((uint64_t)n * 16, 1u << 20);
+    return dbg ? dbg : std::min<uint64_t>(std::max<uint64_t>((uint64_t)n * 160, 1u << 22), 1ull << 31);
 }
 inline uint64_t initial_log_entries(uint32_t n, uint32_t B)
 {

@@ -595,14 +595,23 @@ int pado_server_replay(pado_server *S, uint64_t nreq, const double *arrival_s, c
                 S->cv_done.wait(lk, [&] { return reqs[i].done.load(std::memory_order_acquire) != 0; });
         } else {
             // unbatched: each request copied, launched and read back on its own,
-            // in arrival order (a FIFO server doing one launch per request)
-            cudaSetDevice(S->device);
-            Slot &sl = S->slots[0];
-            {
-                // the dispatcher must be idle: this path uses slot 0 directly
-                std::lock_guard<std::mutex> lk(S->mu);
-                if (!S->q.empty()) throw pado::Error(PADO_E_STATE, "unbatched replay needs an idle server");
-            }
+            // in arrival order (a FIFO server doing one launch per request), with
+            // buffers of its own so the dispatcher's slots are never shared
+            PADO_CUDA(cudaSetDevice(S->device));
+            Slot sl;
+            sl.ha.alloc(S->max_pairs);
+            sl.hb.alloc(S->max_pairs);
+            sl.hout.alloc((uint64_t)S->max_pairs * 2);
+            sl.da.alloc(S->max_pairs);
+            sl.db.alloc(S->max_pairs);
+            sl.dout.alloc((uint64_t)S->max_pairs * 2);
+            PADO_CUDA(cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking));
+            struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{sl.s};
+            struct RefGuard {  // drop in-flight references if a request fails midway
+                pado_server *S;
+                Slot &sl;
+                ~RefGuard() { S->release(sl); }
+            } rg{S, sl};
             for (uint64_t i = 0; i < nreq; ++i) {
                 Req &r = reqs[i];
                 r.t_arrival = t0 + arrival_s[i];

@@ -15,7 +15,7 @@ namespace pado {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int SMALL_CAP = 256;                 // labels with d < iter staged in smem
+constexpr int SMALL_CAP = 384;                 // labels with d < iter staged in smem per chunk
 constexpr uint32_t HEAVY_DEG = 2048;           // tails this large are processed by a block
 
 struct UnwDev {
@@ -200,10 +200,11 @@ __device__ void mark_phase(const UnwDev &d, const uint32_t *front, uint32_t cnt,
             bool appended = false;
             if (ok && !d.used[t] && d.tail_stamp[t] != lid_cur) {
                 if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) {
-                    if (d.off[t + 1] - d.off[t] >= HEAVY_DEG)
-                        htails[atomicAdd(htails_cnt, 1u)] = t;
+                    const bool heavy = d.off[t + 1] - d.off[t] >= HEAVY_DEG;
+                    if (heavy)
+                        htails[agg_append_by(htails_cnt, 1u)] = t;
                     else
-                        tails[atomicAdd(tails_cnt, 1u)] = t;
+                        tails[agg_append_by(tails_cnt, 0u)] = t;
                     appended = true;
                 }
             }
@@ -226,21 +227,19 @@ __host__ __device__ __forceinline__ uint32_t align16(uint32_t x) { return (x + 1
 struct WarpRegion {
     uint32_t *ind;        // words
     uint16_t *offered;    // B
-    uint8_t *tbpd;        // 64
-    ulonglong2 *tbps;     // 64
     uint32_t *sh;         // SMALL_CAP
     uint8_t *sd;          // SMALL_CAP
-    uint32_t *ctr;        // [0] noff, [1] nsmall
+    uint32_t *ctr;        // [0] noff
 };
 
 __host__ __device__ __forceinline__ uint32_t warp_region_bytes(uint32_t words, uint32_t B)
 {
-    return align16(words * 4) + align16(B * 2) + 64 + 64 * 16 + SMALL_CAP * 4 + SMALL_CAP + 16;
+    return align16(words * 4) + align16(B * 2) + SMALL_CAP * 4 + SMALL_CAP + 16;
 }
 
 __host__ __device__ __forceinline__ uint32_t heavy_region_bytes(uint32_t words, uint32_t B)
 {
-    return align16(words * 4) + 2 * align16(B * 2) + 64 + 64 * 16 + HSMALL_CAP * 4 + HSMALL_CAP + 64;
+    return align16(words * 4) + 2 * align16(B * 2) + HSMALL_CAP * 4 + HSMALL_CAP + 64;
 }
 
 __host__ __device__ __forceinline__ uint32_t pull_smem_bytes(uint32_t words, uint32_t B)
@@ -253,8 +252,6 @@ __device__ __forceinline__ WarpRegion warp_region(unsigned char *base, uint32_t 
 {
     unsigned char *p = base + (size_t)w * warp_region_bytes(words, B);
     WarpRegion r;
-    r.tbps = reinterpret_cast<ulonglong2 *>(p);
-    p += 64 * 16;
     r.ind = reinterpret_cast<uint32_t *>(p);
     p += align16(words * 4);
     r.sh = reinterpret_cast<uint32_t *>(p);
@@ -263,19 +260,15 @@ __device__ __forceinline__ WarpRegion warp_region(unsigned char *base, uint32_t 
     p += 16;
     r.offered = reinterpret_cast<uint16_t *>(p);
     p += align16(B * 2);
-    r.tbpd = p;
-    p += 64;
     r.sd = p;
     return r;
 }
 
 struct HeavyRegion {
-    ulonglong2 *tbps;
     uint32_t *ind;
     uint32_t *sh;
     uint16_t *offered;
     uint16_t *surv;
-    uint8_t *tbpd;
     uint8_t *sd;
     uint32_t *ctr;                   // noff, nsurv, nsmall, nadd, mn, ok, reloc, ncap
     unsigned long long *base;
@@ -284,8 +277,6 @@ struct HeavyRegion {
 __device__ __forceinline__ HeavyRegion heavy_region(unsigned char *p, uint32_t words, uint32_t B)
 {
     HeavyRegion r;
-    r.tbps = reinterpret_cast<ulonglong2 *>(p);
-    p += 64 * 16;
     r.base = reinterpret_cast<unsigned long long *>(p);
     p += 16;
     r.ctr = reinterpret_cast<uint32_t *>(p);
@@ -298,8 +289,6 @@ __device__ __forceinline__ HeavyRegion heavy_region(unsigned char *p, uint32_t w
     p += align16(B * 2);
     r.surv = reinterpret_cast<uint16_t *>(p);
     p += align16(B * 2);
-    r.tbpd = p;
-    p += 64;
     r.sd = p;
     return r;
 }
@@ -387,12 +376,13 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         uint32_t mask = __ballot_sync(FULL, act);
         if (lane == 0) bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull;
         else { __ballot_sync(FULL, in); __ballot_sync(FULL, ge); }
+        const uint64_t mpos = act ? d.last_pos[pp][h] : 0ull;
+        const uint32_t mcnt = act ? d.last_cnt[pp][h] : 0u;
         while (mask) {
             const int src = __ffs(mask) - 1;
             mask &= mask - 1;
-            const uint32_t hh = __shfl_sync(FULL, h, src);
-            const uint64_t pos = d.last_pos[pp][hh];
-            const uint32_t c = d.last_cnt[pp][hh];
+            const uint64_t pos = __shfl_sync(FULL, mpos, src);
+            const uint32_t c = __shfl_sync(FULL, mcnt, src);
             if (lane == 0) bytes += 12 + 4ull * c;
             for (uint32_t j = lane; j < c; j += 32) {
                 const uint32_t r = d.pool_hub[pos + j];
@@ -581,12 +571,14 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         const bool act = ge && d.act_stamp[pp][h] == lid_prev;
         uint32_t mask = __ballot_sync(FULL, act);
         bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull;
+        // every active head's last-group position and size, loaded in parallel
+        const uint64_t mpos = act ? d.last_pos[pp][h] : 0ull;
+        const uint32_t mcnt = act ? d.last_cnt[pp][h] : 0u;
         while (mask) {
             const int src = __ffs(mask) - 1;
             mask &= mask - 1;
-            const uint32_t hh = __shfl_sync(FULL, h, src);
-            const uint64_t pos = d.last_pos[pp][hh];
-            const uint32_t c = d.last_cnt[pp][hh];
+            const uint64_t pos = __shfl_sync(FULL, mpos, src);
+            const uint32_t c = __shfl_sync(FULL, mcnt, src);
             bytes += 12 + 4ull * c;  // last-group position/count and its hubs
             for (uint32_t j = lane; j < c; j += 32) {
                 const uint32_t r = d.pool_hub[pos + j];
@@ -651,48 +643,68 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         nsurv = n2;
     }
     tick(W_CYC_BP);
-    // (d) distance test against t's labels with d < iter
+    // (d) distance test against t's labels with d < iter.  Those labels are
+    // staged in shared memory SMALL_CAP at a time (ballot compaction, in list
+    // order); when they all fit, one staging serves every candidate group.
     uint32_t nadd = 0;
     const uint32_t len = d.lab_len[t];
     uint64_t base = d.lab_off[t];
     if (nsurv) {
-        if (lane == 0) wr.ctr[1] = 0;
-        __syncwarp();
-        for (uint32_t j = lane; j < len; j += 32) {
-            const uint8_t dd = d.pool_dist[base + j];
-            if (dd < iter) {
-                const uint32_t slot = atomicAdd(&wr.ctr[1], 1u);
-                if (slot < SMALL_CAP) {
-                    wr.sh[slot] = d.pool_hub[base + j];
-                    wr.sd[slot] = dd;
+        uint32_t nst = 0;
+        // stage labels with d < iter from list position `from`; returns where it stopped
+        auto stage = [&](uint32_t from) -> uint32_t {
+            uint32_t cnt = 0, j = from;
+            for (; j < len && cnt + 32 <= (uint32_t)SMALL_CAP; j += 32) {
+                const uint32_t jj = j + lane;
+                const bool in = jj < len;
+                const uint8_t dd = in ? d.pool_dist[base + jj] : (uint8_t)U8_INF;
+                const bool sm = in && dd < iter;
+                const uint32_t m = __ballot_sync(FULL, sm);
+                if (sm) {
+                    const uint32_t p = cnt + __popc(m & ((1u << lane) - 1u));
+                    wr.sh[p] = d.pool_hub[base + jj];
+                    wr.sd[p] = dd;
                 }
+                cnt += __popc(m);
             }
-        }
-        __syncwarp();
-        const uint32_t nsmall = wr.ctr[1];
-        bytes += 12 + (uint64_t)len + 4ull * min(nsmall, (uint32_t)SMALL_CAP) + (uint64_t)nsurv * nsmall;
+            __syncwarp();
+            nst = cnt;
+            bytes += (uint64_t)min(j, len) - from + 4ull * cnt;
+            return min(j, len);
+        };
+        uint32_t next = stage(0);
+        const bool whole = next >= len;
+        bytes += 12;
         for (uint32_t c0 = 0; c0 < nsurv; c0 += 32) {
             const uint32_t c = c0 + lane;
-            bool keep = false;
-            uint16_t idx = 0;
-            if (c < nsurv) {
-                idx = wr.offered[c];
-                const uint32_t rr = s + idx;
-                const uint8_t *row = bc.dm + (uint64_t)idx * bc.dn;
-                keep = true;
-                if (nsmall <= SMALL_CAP) {
-                    for (uint32_t k = 0; k < nsmall; ++k) {
-                        const uint32_t hh = wr.sh[k];
-                        if (hh < rr && (uint32_t)wr.sd[k] + (uint32_t)row[hh - bc.base] <= iter) { keep = false; break; }
+            bool keep = c < nsurv;
+            const uint16_t idx = keep ? wr.offered[c] : (uint16_t)0;
+            const uint32_t rr = s + idx;
+            const uint8_t *row = bc.dm + (uint64_t)idx * bc.dn - bc.base;  // row[h] for a hub h of this graph
+            if (!whole && c0 > 0) next = stage(0);
+            for (;;) {
+                if (keep) {
+                    uint32_t k = 0;
+                    // four dist_matrix gathers in flight per lane
+                    for (; k + 4 <= nst; k += 4) {
+                        const uint32_t h0 = wr.sh[k], h1 = wr.sh[k + 1], h2 = wr.sh[k + 2], h3 = wr.sh[k + 3];
+                        const uint32_t v0 = row[h0], v1 = row[h1], v2 = row[h2], v3 = row[h3];
+                        if ((h0 < rr && (uint32_t)wr.sd[k] + v0 <= iter) ||
+                            (h1 < rr && (uint32_t)wr.sd[k + 1] + v1 <= iter) ||
+                            (h2 < rr && (uint32_t)wr.sd[k + 2] + v2 <= iter) ||
+                            (h3 < rr && (uint32_t)wr.sd[k + 3] + v3 <= iter)) {
+                            keep = false;
+                            break;
+                        }
                     }
-                } else {
-                    for (uint32_t j = 0; j < len; ++j) {
-                        const uint32_t dd = d.pool_dist[base + j];
-                        if (dd >= iter) continue;
-                        const uint32_t hh = d.pool_hub[base + j];
-                        if (hh < rr && dd + (uint32_t)row[hh - bc.base] <= iter) { keep = false; break; }
+                    for (; keep && k < nst; ++k) {
+                        const uint32_t hh = wr.sh[k];
+                        if (hh < rr && (uint32_t)wr.sd[k] + (uint32_t)row[hh] <= iter) keep = false;
                     }
                 }
+                bytes += (uint64_t)__popc(__ballot_sync(FULL, c < nsurv)) * nst;
+                if (whole || next >= len || !__any_sync(FULL, keep)) break;
+                next = stage(next);
             }
             const uint32_t km = __ballot_sync(FULL, keep);
             __syncwarp();

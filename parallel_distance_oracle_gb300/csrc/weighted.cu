@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256) w_mark_kernel(WDev d, const uint32_t *fro
             const uint32_t t = in ? d.adj[e] : 0u;
             const bool ok = in && t > mn;
             if (ok && d.tail_stamp[t] != lid_cur) {
-                if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) tails[atomicAdd(tails_cnt, 1u)] = t;
+                if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) tails[agg_append(tails_cnt)] = t;
             }
             if (__ballot_sync(FULL, in && !ok)) break;
         }

@@ -12,7 +12,9 @@ Errors raise :class:`PadoError` instead of the reference's print-and-exit.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -54,6 +56,11 @@ class _Index:
     # -- lifetime -----------------------------------------------------------
     def close(self) -> None:
         if getattr(self, "_h", None):
+            # a server that borrows this handle must let go of it first
+            for ref in getattr(self, "_servers", ()):
+                srv = ref()
+                if srv is not None:
+                    srv.close()
             lib.pado_free(self._h)
             self._h = None
 
@@ -231,6 +238,18 @@ def tune_batch(graphs, ranks=None, bp_roots: int = 50, candidates=(256, 512, 102
 
 
 _PADO_E_TIMEOUT = 6
+_live_servers = weakref.WeakSet()
+
+
+@atexit.register
+def _close_servers():
+    # stop every dispatcher thread while the interpreter and the CUDA runtime
+    # are still fully alive
+    for srv in list(_live_servers):
+        try:
+            srv.close()
+        except Exception:
+            pass
 
 
 class Server:
@@ -244,12 +263,15 @@ class Server:
         check(lib.pado_server_create(int(hbm_budget_bytes), max_batch_pairs, slots, C.byref(h)))
         self._h = h
         self._kinds = []
+        self._held = []  # borrowed indexes stay alive until the server is destroyed
         self._pending = {}
+        _live_servers.add(self)
 
     def close(self) -> None:
         if getattr(self, "_h", None):
             lib.pado_server_destroy(self._h)
             self._h = None
+            self._held = []
 
     def __del__(self):
         try:
@@ -261,12 +283,17 @@ class Server:
         i = C.c_uint32()
         check(lib.pado_server_add(self._h, index._need(), C.byref(i)))
         self._kinds.append(index.kind)
+        self._held.append(index)
+        if not hasattr(index, "_servers"):
+            index._servers = []
+        index._servers.append(weakref.ref(self))
         return int(i.value)
 
     def submit(self, index_id: int, a, b) -> int:
         """Queue a request; returns a ticket for ``wait``."""
         a, b = _u32(a), _u32(b)
-        out = np.empty(a.shape, np.uint8 if self._kinds[index_id] == PADO_UNWEIGHTED else np.int16)
+        kind = self._kinds[index_id] if 0 <= index_id < len(self._kinds) else PADO_UNWEIGHTED
+        out = np.empty(a.shape, np.uint8 if kind == PADO_UNWEIGHTED else np.int16)
         t = C.c_uint64()
         check(lib.pado_server_submit(self._h, index_id, a.size, ptr(a), ptr(b), ptr(out), C.byref(t)))
         self._pending[int(t.value)] = (a, b, out)

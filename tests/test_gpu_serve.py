@@ -148,6 +148,8 @@ def test_eviction_and_readmission_keep_results(pado, indexes):
 def test_offloaded_handle_refuses_direct_queries(pado, indexes):
     from parallel_distance_oracle_gb300 import _lib
     (g0, ix0), (g1, ix1) = indexes[0], indexes[1]
+    qa, qb = np.arange(50, dtype=np.uint32), np.arange(50, dtype=np.uint32)[::-1].copy()
+    before = ix0.query(qa, qb)
     budget = max(ix0.info().device_bytes, ix1.info().device_bytes) + 1
     srv = pado.Server(hbm_budget_bytes=budget)
     srv.add(ix0)
@@ -156,12 +158,14 @@ def test_offloaded_handle_refuses_direct_queries(pado, indexes):
     with pytest.raises(_lib.PadoError, match="offloaded"):
         ix0.query(np.array([0], np.uint32), np.array([1], np.uint32))
     srv.close()
-    assert ix0.query(np.array([0], np.uint32), np.array([0], np.uint32))[0] == 0
+    assert np.array_equal(ix0.query(qa, qb), before)
 
 
 def test_bad_requests(pado, indexes):
     from parallel_distance_oracle_gb300 import _lib
     g, ix = indexes[0]
+    qa, qb = np.arange(50, dtype=np.uint32), np.arange(50, dtype=np.uint32)[::-1].copy()
+    before = ix.query(qa, qb)
     srv = pado.Server(hbm_budget_bytes=ix.info().device_bytes - 1)
     i = srv.add(ix)  # larger than the budget: offloaded at once, requests fail
     with pytest.raises(_lib.PadoError):
@@ -169,4 +173,4 @@ def test_bad_requests(pado, indexes):
     with pytest.raises(_lib.PadoError, match="unknown index"):
         srv.submit(99, np.array([0], np.uint32), np.array([1], np.uint32))
     srv.close()
-    assert ix.query(np.array([1], np.uint32), np.array([1], np.uint32))[0] == 0
+    assert np.array_equal(ix.query(qa, qb), before)
