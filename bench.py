@@ -49,10 +49,10 @@ WORKLOADS = {
 }
 # Many independent graphs labeled together: 512 graphs, n log-uniform in
 # [1,000, n_hi], half Erdos-Renyi (average degree 6), half 2D grids with 2%
-# random long-range edges, each degree-ordered, 64 BP roots.  The batch size
+# random long-range edges, each degree-ordered, 50 BP roots.  The batch size
 # is tuned over {256, 512, 1024, 2048} on a size-stratified sample, then the
 # batched build is compared with labeling the graphs one at a time.
-MANY = dict(graphs=512, n_lo=1000, n_hi=20000, er_degree=6, grid_frac=0.02, K=64, seed=5,
+MANY = dict(graphs=512, n_lo=1000, n_hi=20000, er_degree=6, grid_frac=0.02, K=50, seed=5,
             candidates=(256, 512, 1024, 2048), tune_sample=64)
 # Serving: label sets of the R-MAT s20 graph and 64 of the many-graph
 # workload's graphs in HBM under a 40 GB admission budget; open-loop Poisson

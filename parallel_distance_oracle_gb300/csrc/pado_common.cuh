@@ -185,13 +185,13 @@ inline uint64_t debug_pool_entries()
     const char *e = std::getenv("PADO_DEBUG_POOL_ENTRIES");
     return e ? std::strtoull(e, nullptr, 10) : 0;
 }
-// The label pool starts at 160 entries per vertex (0.8 KB/vertex unweighted,
+// The label pool starts at 256 entries per vertex (1.3 KB/vertex unweighted,
 // capped at 2^31 entries): enough for a social-graph labeling plus its list
 // relocations in one persistent launch, so growth relaunches are rare.
 inline uint64_t initial_pool_entries(uint32_t n)
 {
     const uint64_t dbg = debug_pool_entries();
-    return dbg ? dbg : std::min<uint64_t>(std::max<uint64_t>((uint64_t)n * 160, 1u << 22), 1ull << 31);
+    return dbg ? dbg : std::min<uint64_t>(std::max<uint64_t>((uint64_t)n * 256, 1u << 22), 1ull << 31);
 }
 inline uint64_t initial_log_entries(uint32_t n, uint32_t B)
 {

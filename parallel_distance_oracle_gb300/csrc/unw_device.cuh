@@ -320,6 +320,39 @@ __device__ __forceinline__ bool bp_covered_warp(const UnwDev &d, uint32_t r, int
     return __ballot_sync(FULL, cov) != 0;
 }
 
+// The same test for two candidates at once (rb only if `two`), distances
+// first: a root's 16-byte sets are loaded only where its distance sum can
+// prune (x - 2 <= iter), so sparse graphs, where BP distances are mostly too
+// large, read 64 bytes per candidate instead of 1 KB.  Bit 0: ra covered,
+// bit 1: rb covered.
+__device__ __forceinline__ uint32_t bp_covered_pair(const UnwDev &d, uint32_t ra, uint32_t rb, bool two, int lane,
+                                                    uint32_t skip, uint8_t td0, ulonglong2 ts0, uint8_t td1,
+                                                    ulonglong2 ts1, uint32_t iter)
+{
+    const uint32_t K = d.K, i0 = lane, i1 = lane + 32;
+    const bool v0 = i0 >= skip && i0 < K, v1 = i1 >= skip && i1 < K;
+    const uint8_t *da = d.bpd + (uint64_t)ra * K, *db = d.bpd + (uint64_t)rb * K;
+    const uint32_t xa0 = v0 ? (uint32_t)da[i0] + td0 : 0u, xa1 = v1 ? (uint32_t)da[i1] + td1 : 0u;
+    const uint32_t xb0 = two && v0 ? (uint32_t)db[i0] + td0 : 0u, xb1 = two && v1 ? (uint32_t)db[i1] + td1 : 0u;
+    // x == 0 (unused lane) fails the test like x < 2 does in bp_one
+    const bool na0 = xa0 - 2u <= iter, na1 = xa1 - 2u <= iter, nb0 = xb0 - 2u <= iter, nb1 = xb1 - 2u <= iter;
+    const ulonglong2 *sa = reinterpret_cast<const ulonglong2 *>(d.bps) + (uint64_t)ra * K;
+    const ulonglong2 *sb = reinterpret_cast<const ulonglong2 *>(d.bps) + (uint64_t)rb * K;
+    auto cut = [&](uint32_t x, ulonglong2 rs, ulonglong2 ts) {
+        if (rs.x & ts.x)
+            x -= 2u;
+        else if ((rs.x & ts.y) | (rs.y & ts.x))
+            x -= 1u;
+        return x <= iter;
+    };
+    bool ca = false, cb = false;
+    if (na0) ca = cut(xa0, sa[i0], ts0);
+    if (na1) ca = ca || cut(xa1, sa[i1], ts1);
+    if (nb0) cb = cut(xb0, sb[i0], ts0);
+    if (nb1) cb = cb || cut(xb1, sb[i1], ts1);
+    return (__ballot_sync(FULL, ca) ? 1u : 0u) | (__ballot_sync(FULL, cb) ? 2u : 0u);
+}
+
 struct PullArgs {
     const uint32_t *tails;        // light tails
     const uint32_t *tails_cnt;
@@ -561,19 +594,10 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     for (uint32_t x = lane; x < d.words; x += 32) wr.ind[x] = valid ? d.ind[(uint64_t)t * d.words + x] : 0u;
     if (lane == 0) wr.ctr[0] = 0;
     __syncwarp();
-    // (b) gather first offers from active neighbours (heads >= s)
+    // (b) gather first offers from active neighbours (heads >= s), 64
+    // neighbours per step so that two chunks' gathers are in flight at once
     const uint32_t e_end = d.off[t + 1];
-    for (uint32_t e0 = d.off[t]; e0 < e_end; e0 += 32) {
-        const uint32_t e = e0 + lane;
-        const bool in = e < e_end;
-        const uint32_t h = in ? d.adj[e] : 0u;
-        const bool ge = in && h >= s;
-        const bool act = ge && d.act_stamp[pp][h] == lid_prev;
-        uint32_t mask = __ballot_sync(FULL, act);
-        bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull;
-        // every active head's last-group position and size, loaded in parallel
-        const uint64_t mpos = act ? d.last_pos[pp][h] : 0ull;
-        const uint32_t mcnt = act ? d.last_cnt[pp][h] : 0u;
+    auto offer_from = [&](uint32_t mask, uint64_t mpos, uint32_t mcnt) {
         while (mask) {
             const int src = __ffs(mask) - 1;
             mask &= mask - 1;
@@ -590,7 +614,23 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
                 }
             }
         }
-        if (__ballot_sync(FULL, in && !ge)) break;
+    };
+    for (uint32_t e0 = d.off[t]; e0 < e_end; e0 += 64) {
+        const uint32_t ea = e0 + lane, eb = ea + 32;
+        const bool ina = ea < e_end, inb = eb < e_end;
+        const uint32_t ha = ina ? d.adj[ea] : 0u, hb = inb ? d.adj[eb] : 0u;
+        const bool gea = ina && ha >= s, geb = inb && hb >= s;
+        const bool acta = gea && d.act_stamp[pp][ha] == lid_prev;
+        const bool actb = geb && d.act_stamp[pp][hb] == lid_prev;
+        // every active head's last-group position and size, loaded in parallel
+        const uint64_t pa = acta ? d.last_pos[pp][ha] : 0ull, pb = actb ? d.last_pos[pp][hb] : 0ull;
+        const uint32_t ca = acta ? d.last_cnt[pp][ha] : 0u, cb = actb ? d.last_cnt[pp][hb] : 0u;
+        bytes += __popc(__ballot_sync(FULL, ina)) * 4ull + __popc(__ballot_sync(FULL, gea)) * 4ull +
+                 __popc(__ballot_sync(FULL, inb)) * 4ull + __popc(__ballot_sync(FULL, geb)) * 4ull;
+        offer_from(__ballot_sync(FULL, acta), pa, ca);
+        offer_from(__ballot_sync(FULL, actb), pb, cb);
+        // descending list: once a neighbour is < s, the rest are too
+        if (__ballot_sync(FULL, (ina && !gea) || (inb && !geb))) break;
     }
     __syncwarp();
     const uint32_t noff = wr.ctr[0];
@@ -630,8 +670,8 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             const uint16_t ia = wr.offered[c];
             const bool two = c + 1 < nsurv;
             const uint16_t ib = two ? wr.offered[c + 1] : ia;
-            const bool ca = bp_covered_warp(d, s + ia, lane, 1, td0, ts0, td1, ts1, iter);
-            const bool cb = two && bp_covered_warp(d, s + ib, lane, 1, td0, ts0, td1, ts1, iter);
+            const uint32_t cov = bp_covered_pair(d, s + ia, s + ib, two, lane, 1, td0, ts0, td1, ts1, iter);
+            const bool ca = cov & 1u, cb = two && (cov & 2u);
             __syncwarp();
             if (lane == 0) {
                 if (!ca) wr.offered[n2] = ia;
