@@ -58,7 +58,7 @@ MANY = dict(graphs=512, n_lo=1000, n_hi=20000, er_degree=6, grid_frac=0.02, K=50
 # workload's graphs in HBM under a 40 GB admission budget; open-loop Poisson
 # arrivals; each request asks one label set (uniform) for k pairs, k
 # log-uniform in [1, 65536], endpoints Zipf(1.1) over degree rank.
-SERVE = dict(budget=40 << 30, graphs=64, kmax=65536, zipf=1.1, rates=(1e4, 3e4, 5e4, 1e5, 3e5, 1e6, 1e7),
+SERVE = dict(budget=40 << 30, graphs=64, kmax=65536, zipf=1.1, rates=(1e4, 3e4, 5e4, 1e5, 1.5e5, 2e5, 3e5, 1e6, 1e7),
              pairs_per_rate=40_000_000, max_batch_pairs=1 << 18, slots=8, seed=9)
 METRIC = "labels_per_s"
 UNIT = "labels/s"
@@ -645,8 +645,10 @@ def run_serve(args):
         "peak_batched_queries_per_s": peak_b["batched"]["queries_per_s"],
         "sweep": sweep, "server_stats": stats, "clocks": clocks, "gpu_launches": launches,
         "e2e": {"value": best["batched"]["queries_per_s"] if best else None, "unit": "queries/s",
-                "h2d_bytes_per_step": 8, "d2h_bytes_per_step": 1,
-                "note": "per pair, host arrays in and out through pado_server_replay"},
+                "h2d_bytes_per_step": int(8 * best["pairs"] / best["requests"]) if best else None,
+                "d2h_bytes_per_step": int(best["pairs"] / best["requests"]) if best else None,
+                "note": "a step is one request: its pairs in from host arrays, its distances back, "
+                        "through pado_server_replay"},
     }
     print(json.dumps(out), flush=True)
 

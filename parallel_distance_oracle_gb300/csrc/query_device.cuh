@@ -68,30 +68,16 @@ __device__ __forceinline__ uint8_t query_unw_pair(const IndexView &v, uint32_t x
     if (x >= v.n || y >= v.n) return (x == y) ? 0 : U8_INF;
     const uint32_t rx = v.rank ? v.rank[x] : x;
     const uint32_t ry = v.rank ? v.rank[y] : y;
-    // BP part, distances first.  A root takes part when td_i - 2 <= 255
-    // (td_i in [2, 257], unsigned as in the reference).  With t0 = the least
-    // td_i among those, a root whose td_i exceeds t0 + 2 cannot beat the root
-    // that gives t0 (the set adjustment is at most -2), so only roots with
-    // td_i <= t0 + 2 need their 16-byte sets.  The result is the reference's
-    // sequential min exactly.
-    uint32_t td[2] = {0xffffu, 0xffffu};
-    uint32_t t0 = 0xffffu;
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const uint32_t i = lane + 32 * k;
-        if (i < v.K) td[k] = (uint32_t)v.bpd[(uint64_t)rx * v.K + i] + (uint32_t)v.bpd[(uint64_t)ry * v.K + i];
-        if (td[k] - 2u <= (uint32_t)U8_INF) t0 = min(t0, td[k]);
-    }
-    t0 = warp_min(t0);
+    // BP part: lane i takes roots i and i + 32, sets loaded with the distances
+    // (one round trip); a root takes part when td - 2 <= 255 (unsigned).
     uint32_t d = U8_INF;
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const uint32_t i = lane + 32 * k;
-        if (i < v.K && td[k] - 2u <= (uint32_t)U8_INF && td[k] <= t0 + 2u) {
-            const ulonglong2 sx = *reinterpret_cast<const ulonglong2 *>(v.bps + ((uint64_t)rx * v.K + i) * 2);
-            const ulonglong2 sy = *reinterpret_cast<const ulonglong2 *>(v.bps + ((uint64_t)ry * v.K + i) * 2);
+    for (uint32_t i = lane; i < v.K; i += 32) {
+        const uint32_t td = (uint32_t)v.bpd[(uint64_t)rx * v.K + i] + (uint32_t)v.bpd[(uint64_t)ry * v.K + i];
+        const ulonglong2 sx = *reinterpret_cast<const ulonglong2 *>(v.bps + ((uint64_t)rx * v.K + i) * 2);
+        const ulonglong2 sy = *reinterpret_cast<const ulonglong2 *>(v.bps + ((uint64_t)ry * v.K + i) * 2);
+        if (td - 2u <= (uint32_t)U8_INF) {
             const uint32_t adj = (sx.x & sy.x) ? 2u : (((sx.x & sy.y) | (sx.y & sy.x)) ? 1u : 0u);
-            const uint32_t t = td[k] - adj;
+            const uint32_t t = td - adj;
             d = t < d ? t : d;
         }
     }

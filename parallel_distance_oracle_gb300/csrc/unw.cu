@@ -108,6 +108,8 @@ struct LoopBufs {
     uint32_t *front[2];
     uint32_t *tails, *htails, *retry;
     unsigned long long *batch_ns;  // optional per-batch end time (trace)
+    unsigned long long *level_log; // optional per level: end time, tails << 32 | batch (trace)
+    uint32_t level_cap;
     uint32_t nbatches;
 };
 
@@ -203,6 +205,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 4) label_loop_kernel(UnwDev d, L
         const uint32_t fn = vload(&c->front_cnt[cp]);
         if (fn == 0) dm_rows_phase(d, bf.roots, vload(&c->nroots[b & 1]), s, 0);
         if (leader) {
+            if (bf.level_log && c->levels < bf.level_cap) {
+                const unsigned long long nt = vload(&c->tails_cnt[cp]) + vload(&c->htails_cnt[cp]);
+                bf.level_log[2ull * c->levels] = gtimer();
+                bf.level_log[2ull * c->levels + 1] = (nt << 32) | b;
+            }
             c->lid = lid_cur;
             c->iter = iter;
             c->levels += 1;
@@ -350,24 +357,27 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
             DBuf<LoopCtl> ctl(1);
             DBuf<uint32_t> rr(B);
             DBuf<unsigned long long> bns(trace ? nbatches : 1);
+            const uint32_t level_cap = trace ? (1u << 22) : 0u;
+            DBuf<unsigned long long> llog(trace ? 2ull * level_cap : 1);
             ctl.fill_bytes(0, s);
             if (trace) bns.fill_bytes(0, s);
             LoopBufs bf{roots.p, rr.p, {front0.p, front1.p}, tails.p, htails.p, retry.p, trace ? bns.p : nullptr,
-                        nbatches};
-            PADO_CUDA(cudaFuncSetAttribute(label_loop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                        trace ? llog.p : nullptr, level_cap, nbatches};
+            const void *kfn = (const void *)label_loop_kernel;
+            PADO_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             int dev = 0, sms = 0, per_sm = 0;
             PADO_CUDA(cudaGetDevice(&dev));
             PADO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            PADO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, label_loop_kernel, PULL_THREADS, smem));
+            PADO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, PULL_THREADS, smem));
             PADO_CHECK(per_sm >= 1, PADO_E_CUDA, "labeling loop kernel cannot be resident");
-            const unsigned grid = (unsigned)(sms * std::min(per_sm, 4));
+            const unsigned grid = (unsigned)(sms * std::min(per_sm, 4));  // compiled for 4 blocks/SM
             LoopCtl h{};
             LoopCtl *cp_ = ctl.p;
             for (int launch = 0;; ++launch) {
                 PADO_CHECK(launch < 256, PADO_E_NOMEM, "label pool could not be grown enough");
                 void *args[] = {&d, &cp_, &bf};
                 PADO_LAUNCH("label_loop_kernel", s,
-                            PADO_CUDA(cudaLaunchCooperativeKernel((void *)label_loop_kernel, grid, PULL_THREADS, args,
+                            PADO_CUDA(cudaLaunchCooperativeKernel(kfn, grid, PULL_THREADS, args,
                                                                   smem, s)));
                 PADO_CUDA(cudaMemcpyAsync(&h, ctl.p, sizeof(LoopCtl), cudaMemcpyDeviceToHost, s));
                 PADO_CUDA(cudaStreamSynchronize(s));
@@ -406,6 +416,26 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
                     if (prev) fprintf(stderr, "batch %u ms %.3f\n", i, (t[i] - prev) * 1e-6);
                     prev = t[i];
                 }
+                // time per level, bucketed by the level's tail count
+                const uint32_t nl = std::min(h.levels, level_cap);
+                std::vector<unsigned long long> lg(2ull * nl);
+                llog.download(lg.data(), lg.size(), s);
+                PADO_CUDA(cudaStreamSynchronize(s));
+                const uint64_t edges[] = {0, 64, 512, 4096, 32768, 262144, ~0ull};
+                double ms[6] = {}, tl[6] = {};
+                uint64_t cnt[6] = {};
+                for (uint32_t i = 1; i < nl; ++i) {
+                    const uint64_t nt = lg[2 * i + 1] >> 32;
+                    int k = 0;
+                    while (nt >= edges[k + 1]) ++k;
+                    ms[k] += (lg[2 * i] - lg[2 * i - 2]) * 1e-6;
+                    tl[k] += (double)nt;
+                    ++cnt[k];
+                }
+                for (int k = 0; k < 6; ++k)
+                    fprintf(stderr, "levels with tails in [%llu, %llu): %llu levels, %.3f ms, %.0f tails\n",
+                            (unsigned long long)edges[k], (unsigned long long)edges[k + 1], (unsigned long long)cnt[k],
+                            ms[k], tl[k]);
             }
         }
         for (uint32_t bs = 0, b = 0; host_loop && bs < n; bs += B, ++b) {

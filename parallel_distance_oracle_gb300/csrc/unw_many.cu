@@ -357,19 +357,20 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
     PADO_CUDA(cudaEventRecord(e0, s));
     try {
         if (active) {
-            PADO_CUDA(cudaFuncSetAttribute(many_loop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            const void *kfn = (const void *)many_loop_kernel;
+            PADO_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             int dev = 0, sms = 0, per_sm = 0;
             PADO_CUDA(cudaGetDevice(&dev));
             PADO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            PADO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, many_loop_kernel, PULL_THREADS, smem));
+            PADO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, PULL_THREADS, smem));
             PADO_CHECK(per_sm >= 1, PADO_E_CUDA, "many-graph labeling kernel cannot be resident");
-            const unsigned grid = (unsigned)(sms * std::min(per_sm, 4));
+            const unsigned grid = (unsigned)(sms * std::min(per_sm, 4));  // compiled for 4 blocks/SM
             ManyCtl *cptr = ctl.p;
             for (int launch = 0;; ++launch) {
                 PADO_CHECK(launch < 256, PADO_E_NOMEM, "label pool could not be grown enough");
                 void *args[] = {&d, &cptr, &bf};
                 PADO_LAUNCH("many_loop_kernel", s,
-                            PADO_CUDA(cudaLaunchCooperativeKernel((void *)many_loop_kernel, grid, PULL_THREADS, args,
+                            PADO_CUDA(cudaLaunchCooperativeKernel(kfn, grid, PULL_THREADS, args,
                                                                   smem, s)));
                 PADO_CUDA(cudaMemcpyAsync(&h, ctl.p, sizeof(ManyCtl), cudaMemcpyDeviceToHost, s));
                 PADO_CUDA(cudaStreamSynchronize(s));
