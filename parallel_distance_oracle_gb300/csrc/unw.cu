@@ -82,8 +82,20 @@ __global__ void __launch_bounds__(PULL_THREADS, 4) pull_kernel(UnwDev d, PullArg
 
 // ---------------------------------------------------------------------------
 // Persistent labeling loop: one cooperative launch runs batch after batch,
-// level after level, with a grid barrier between phases instead of a kernel
-// boundary and a host round trip.  The kernel returns to the host only when
+// level after level, with ONE grid barrier per step:
+//   batch step (batch b at stamp L): each root r of b gets its self label
+//       (stamp L), fills dist_matrix row r - s from its labels and marks its
+//       own tails for L+1; the rows of batch b-1 are reset in the same step
+//       (dist_matrix is double-buffered by batch parity, so the two never
+//       share a row);
+//   level step (stamp L, level iter): pull over the tails marked for L; a
+//       tail that gains labels marks its tails for L+1 at once.
+// After the barrier every block reads the same tail count for L+1 and takes
+// the same decision (no tails: the batch is over -- its next level would add
+// nothing -- and the next step starts batch b+1), so no leader round trip is
+// needed.  Tail lists and their counters rotate over 3 slots by stamp: slot
+// L % 3 is read, (L+1) % 3 is appended to, and (L+2) % 3 -- last read at L-1
+// -- is cleared for the step after.  The kernel returns to the host only when
 // every batch is done, when the label pool must grow (a warp could not
 // reserve space; the failed tails or roots are re-run exactly after the
 // growth), or on an error.  The barrier's spin is bounded: after
@@ -95,90 +107,116 @@ enum LoopExit : uint32_t { EX_RUNNING = 0, EX_DONE = 1, EX_NEED_POOL = 2, EX_OVE
 
 struct LoopCtl {
     GridBar bar;
-    uint32_t phase, b, iter, lid;
-    uint32_t front_cnt[2], tails_cnt[2], htails_cnt[2];
-    uint32_t nroots[2];  // roots of batch b in nroots[b & 1]
+    uint32_t phase, b, iter, lid;       // the step to run next: phase, batch, level, last completed stamp
+    uint32_t tcnt[3], hcnt[3];          // light / heavy tails marked for stamp x, in slot x % 3
     uint32_t rr_cnt, retry_cnt, status, exit_code;
     uint32_t levels, pad;
 };
 
 struct LoopBufs {
-    uint32_t *roots;      // roots of the current batch
-    uint32_t *rr;         // roots to re-run after a pool growth
-    uint32_t *front[2];
-    uint32_t *tails, *htails, *retry;
+    const uint32_t *broots;   // roots of every batch, batch by batch
+    const uint32_t *boff;     // batch b's roots: broots[boff[b], boff[b+1])
+    uint32_t *rr;             // roots to re-run after a pool growth
+    uint32_t *tails[3], *htails[3], *retry;
+    uint8_t *dm[2];           // dist_matrix by batch parity
     unsigned long long *batch_ns;  // optional per-batch end time (trace)
     unsigned long long *level_log; // optional per level: end time, tails << 32 | batch (trace)
     uint32_t level_cap;
     uint32_t nbatches;
 };
 
+// Batch step for roots[0, nr): self label at stamp L, dist_matrix row, tails for L+1.
+__device__ void root_step_phase(const UnwDev &d, const uint32_t *roots, uint32_t nr, uint32_t s, uint32_t b,
+                                uint32_t L, uint8_t *dm, const LoopBufs &bf, LoopCtl *c)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const int p = L & 1, nx = (L + 1) % 3;
+    unsigned long long bytes = 0;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nr; q += nw) {
+        const uint32_t r = roots[q];
+        uint64_t base;
+        if (!warp_reserve(d, r, d.lab_len[r] + 1, base, lane)) {
+            if (lane == 0) {
+                atomicOr(d.status, ST_POOL_RETRY);
+                bf.retry[atomicAdd(&c->retry_cnt, 1u)] = r;
+            }
+            continue;
+        }
+        const uint32_t len = d.lab_len[r];
+        const uint32_t idx = r - s;
+        for (uint32_t w = lane; w < d.words; w += 32)
+            d.ind[(uint64_t)r * d.words + w] = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
+        if (lane == 0) {
+            d.pool_hub[base + len] = r;
+            d.pool_dist[base + len] = 0;
+            d.lab_len[r] = len + 1;
+            d.last_pos[p][r] = base + len;
+            d.last_cnt[p][r] = 1;
+            d.last_min[p][r] = r;
+            d.act_stamp[p][r] = L;
+            d.ind_stamp[r] = b + 1;
+        }
+        __syncwarp();
+        // dist_matrix row of r from all its labels, the new (r, 0) included
+        uint8_t *row = dm + (uint64_t)idx * d.n;
+        for (uint32_t j = lane; j <= len; j += 32) row[d.pool_hub[base + j]] = d.pool_dist[base + j];
+        mark_tails(d, r, r, L + 1, bf.tails[nx], &c->tcnt[nx], bf.htails[nx], &c->hcnt[nx], lane, 0, 1, bytes);
+    }
+    if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_MARK], bytes);
+}
+
 __global__ void __launch_bounds__(PULL_THREADS, 4) label_loop_kernel(UnwDev d, LoopCtl *c, LoopBufs bf)
 {
     extern __shared__ __align__(16) unsigned char pull_smem[];
     const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+    // the loop state lives in registers; every block derives the same
+    // transitions from the same post-barrier counters
+    uint32_t phase = vload(&c->phase), b = vload(&c->b), iter = vload(&c->iter), L = vload(&c->lid) + 1;
+    uint32_t levels = vload(&c->levels);
     for (;;) {
-        const uint32_t phase = vload(&c->phase);
-        const uint32_t b = vload(&c->b);
-        if (phase == PH_DONE) return;
-        if (b >= bf.nbatches) {
-            if (leader) {
-                c->phase = PH_DONE;
-                c->exit_code = EX_DONE;
-            }
-            return;
-        }
-        const uint32_t s = b * d.B;
-        const uint32_t e = (uint32_t)min((uint64_t)s + d.B, (uint64_t)d.n);
         if (phase == PH_BATCH || phase == PH_ROOT_RETRY) {
-            const uint32_t lid0 = vload(&c->lid) + 1;
-            const int p0 = lid0 & 1;
+            if (b >= bf.nbatches) break;
+            const uint32_t s = b * d.B;
+            uint8_t *dm = bf.dm[b & 1];
             if (phase == PH_BATCH) {
-                for (uint32_t r = s + blockIdx.x * blockDim.x + threadIdx.x; r < e; r += gridDim.x * blockDim.x)
-                    if (!d.used[r]) bf.roots[atomicAdd(&c->nroots[b & 1], 1u)] = r;
-                if (!grid_barrier(&c->bar, &c->status)) return;
-                const uint32_t nr = vload(&c->nroots[b & 1]);
-                if (nr == 0) {  // every vertex of this batch is a BP vertex
-                    if (!grid_barrier(&c->bar, &c->status)) return;
-                    if (leader) {
-                        c->b = b + 1;
-                        c->nroots[(b + 1) & 1] = 0;
-                    }
-                    if (!grid_barrier(&c->bar, &c->status)) return;
-                    continue;
-                }
-                root_init_phase(d, bf.roots, nr, s, b, lid0, bf.front[p0], &c->front_cnt[p0], bf.retry,
-                                &c->retry_cnt);
+                // rows of the previous batch go back to 255 (other parity)
+                if (b > 0)
+                    dm_rows_phase(d, bf.broots + bf.boff[b - 1], bf.boff[b] - bf.boff[b - 1], s - d.B, 0,
+                                  nullptr, nullptr, bf.dm[(b - 1) & 1]);
+                root_step_phase(d, bf.broots + bf.boff[b], bf.boff[b + 1] - bf.boff[b], s, b, L, dm, bf, c);
             } else {
-                root_init_phase(d, bf.rr, vload(&c->rr_cnt), s, b, lid0, bf.front[p0], &c->front_cnt[p0], bf.retry,
-                                &c->retry_cnt);
+                root_step_phase(d, bf.rr, vload(&c->rr_cnt), s, b, L, dm, bf, c);
+            }
+            if (leader) {
+                c->tcnt[(L + 2) % 3] = 0;
+                c->hcnt[(L + 2) % 3] = 0;
             }
             if (!grid_barrier(&c->bar, &c->status)) return;
             if (vload(&c->retry_cnt)) {
                 if (leader) {
                     c->phase = PH_ROOT_RETRY;
+                    c->b = b;
+                    c->iter = 0;
+                    c->lid = L - 1;
+                    c->levels = levels;
                     c->exit_code = EX_NEED_POOL;
                 }
                 return;
             }
-            dm_rows_phase(d, bf.roots, vload(&c->nroots[b & 1]), s, 1);
-            if (leader) {
-                const int p1 = (lid0 + 1) & 1;
-                c->nroots[(b + 1) & 1] = 0;  // next batch's count; nobody reads it until then
-                c->lid = lid0;
-                c->iter = 0;
-                c->tails_cnt[p1] = 0;
-                c->htails_cnt[p1] = 0;
-                c->front_cnt[p1] = 0;
-                c->phase = PH_LEVEL;
+            const uint32_t nt = vload(&c->tcnt[(L + 1) % 3]) + vload(&c->hcnt[(L + 1) % 3]);
+            if (nt == 0) {  // no tails: nothing can change in this batch
+                if (leader && bf.batch_ns) bf.batch_ns[b] = gtimer();
+                ++b;
+                phase = PH_BATCH;
+            } else {
+                iter = 1;
+                phase = PH_LEVEL;
             }
-            if (!grid_barrier(&c->bar, &c->status)) return;
+            ++L;
             continue;
         }
-        // PH_LEVEL / PH_PULL_RETRY
-        const uint32_t lid_cur = vload(&c->lid) + 1;
-        const uint32_t iter = vload(&c->iter) + 1;
-        const int pp = (lid_cur - 1) & 1, cp = lid_cur & 1;
+        // PH_LEVEL / PH_PULL_RETRY: level iter of batch b at stamp L
         if (iter >= U8_INF) {
             if (leader) {
                 c->phase = PH_DONE;
@@ -186,45 +224,57 @@ __global__ void __launch_bounds__(PULL_THREADS, 4) label_loop_kernel(UnwDev d, L
             }
             return;
         }
-        if (phase == PH_LEVEL) {
-            mark_phase(d, bf.front[pp], vload(&c->front_cnt[pp]), lid_cur, bf.tails, &c->tails_cnt[cp], bf.htails,
-                       &c->htails_cnt[cp]);
-            if (!grid_barrier(&c->bar, &c->status)) return;
-        }
-        PullArgs a{bf.tails, &c->tails_cnt[cp], bf.htails, &c->htails_cnt[cp], s, e, b, iter, lid_cur,
-                   bf.front[cp], &c->front_cnt[cp], bf.retry, &c->retry_cnt};
+        const uint32_t s = b * d.B;
+        const uint32_t e = (uint32_t)min((uint64_t)s + d.B, (uint64_t)d.n);
+        const int cur = L % 3, nx = (L + 1) % 3;
+        PullArgs a{bf.tails[cur], &c->tcnt[cur], bf.htails[cur], &c->hcnt[cur], s, e, b, iter, L,
+                   nullptr, nullptr, bf.retry, &c->retry_cnt};
+        a.next_tails = bf.tails[nx];
+        a.next_tails_cnt = &c->tcnt[nx];
+        a.next_htails = bf.htails[nx];
+        a.next_htails_cnt = &c->hcnt[nx];
+        a.next_stamp = L + 1;
+        a.dm = bf.dm[b & 1];
         pull_phase(d, a, pull_smem);
+        if (leader && phase == PH_LEVEL) {
+            c->tcnt[(L + 2) % 3] = 0;
+            c->hcnt[(L + 2) % 3] = 0;
+        }
         if (!grid_barrier(&c->bar, &c->status)) return;
         if (vload(&c->retry_cnt)) {
             if (leader) {
                 c->phase = PH_PULL_RETRY;
+                c->b = b;
+                c->iter = iter;
+                c->lid = L - 1;
+                c->levels = levels;
                 c->exit_code = EX_NEED_POOL;
             }
             return;
         }
-        const uint32_t fn = vload(&c->front_cnt[cp]);
-        if (fn == 0) dm_rows_phase(d, bf.roots, vload(&c->nroots[b & 1]), s, 0);
-        if (leader) {
-            if (bf.level_log && c->levels < bf.level_cap) {
-                const unsigned long long nt = vload(&c->tails_cnt[cp]) + vload(&c->htails_cnt[cp]);
-                bf.level_log[2ull * c->levels] = gtimer();
-                bf.level_log[2ull * c->levels + 1] = (nt << 32) | b;
-            }
-            c->lid = lid_cur;
-            c->iter = iter;
-            c->levels += 1;
-            c->tails_cnt[pp] = 0;
-            c->htails_cnt[pp] = 0;
-            c->front_cnt[pp] = 0;
-            if (fn == 0) {
-                c->b = b + 1;
-                c->phase = PH_BATCH;
-                if (bf.batch_ns) bf.batch_ns[b] = gtimer();
-            } else {
-                c->phase = PH_LEVEL;
-            }
+        const uint32_t nt = vload(&c->tcnt[nx]) + vload(&c->hcnt[nx]);
+        if (leader && bf.level_log && levels < bf.level_cap) {
+            const unsigned long long tl = vload(&c->tcnt[cur]) + vload(&c->hcnt[cur]);
+            bf.level_log[2ull * levels] = gtimer();
+            bf.level_log[2ull * levels + 1] = (tl << 32) | b;
         }
-        if (!grid_barrier(&c->bar, &c->status)) return;
+        ++levels;
+        if (nt == 0) {
+            if (leader && bf.batch_ns) bf.batch_ns[b] = gtimer();
+            ++b;
+            phase = PH_BATCH;
+        } else {
+            ++iter;
+            phase = PH_LEVEL;
+        }
+        ++L;
+    }
+    if (leader) {
+        c->phase = PH_DONE;
+        c->b = b;
+        c->lid = L - 1;
+        c->levels = levels;
+        c->exit_code = EX_DONE;
     }
 }
 
@@ -354,6 +404,21 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     try {
         if (!host_loop && n) {
             // ---- persistent cooperative loop ----
+            // every batch's roots (non-BP vertices), fixed before labeling starts
+            std::vector<uint32_t> hb_roots, hb_off(nbatches + 1, 0);
+            hb_roots.reserve(n);
+            for (uint32_t b = 0; b < nbatches; ++b) {
+                const uint32_t lo = b * B, hi = (uint32_t)std::min<uint64_t>((uint64_t)lo + B, n);
+                for (uint32_t r = lo; r < hi; ++r)
+                    if (!used[r]) hb_roots.push_back(r);
+                hb_off[b + 1] = (uint32_t)hb_roots.size();
+            }
+            DBuf<uint32_t> d_broots(std::max<size_t>(hb_roots.size(), 1)), d_boff(nbatches + 1);
+            d_broots.upload(hb_roots.data(), hb_roots.size(), s);
+            d_boff.upload(hb_off.data(), nbatches + 1, s);
+            DBuf<uint8_t> dm2((uint64_t)B * n);  // second dist_matrix buffer (odd batches)
+            dm2.fill_bytes(0xff, s);
+            DBuf<uint32_t> tails2(n), htails3(n);
             DBuf<LoopCtl> ctl(1);
             DBuf<uint32_t> rr(B);
             DBuf<unsigned long long> bns(trace ? nbatches : 1);
@@ -361,8 +426,10 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
             DBuf<unsigned long long> llog(trace ? 2ull * level_cap : 1);
             ctl.fill_bytes(0, s);
             if (trace) bns.fill_bytes(0, s);
-            LoopBufs bf{roots.p, rr.p, {front0.p, front1.p}, tails.p, htails.p, retry.p, trace ? bns.p : nullptr,
-                        trace ? llog.p : nullptr, level_cap, nbatches};
+            // tail slots: the three light lists reuse the host loop's front and tail buffers
+            LoopBufs bf{d_broots.p, d_boff.p, rr.p, {tails.p, front0.p, tails2.p}, {htails.p, front1.p, htails3.p},
+                        retry.p, {dm.p, dm2.p}, trace ? bns.p : nullptr, trace ? llog.p : nullptr, level_cap,
+                        nbatches};
             const void *kfn = (const void *)label_loop_kernel;
             PADO_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             int dev = 0, sms = 0, per_sm = 0;
@@ -371,6 +438,7 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
             PADO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, PULL_THREADS, smem));
             PADO_CHECK(per_sm >= 1, PADO_E_CUDA, "labeling loop kernel cannot be resident");
             const unsigned grid = (unsigned)(sms * std::min(per_sm, 4));  // compiled for 4 blocks/SM
+            PADO_CHECK(grid <= BAR_GROUP * BAR_MAX_GROUPS, PADO_E_CUDA, "grid larger than the barrier supports");
             LoopCtl h{};
             LoopCtl *cp_ = ctl.p;
             for (int launch = 0;; ++launch) {
@@ -394,10 +462,12 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
                     PADO_CUDA(cudaMemcpyAsync(rr.p, retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
                     h.rr_cnt = h.retry_cnt;
                 } else {
-                    const int cpar = (h.lid + 1) & 1;
-                    PADO_CUDA(cudaMemcpyAsync(tails.p, retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
-                    h.tails_cnt[cpar] = h.retry_cnt;
-                    h.htails_cnt[cpar] = 0;
+                    // the failed tails become the whole light list of the step (any degree is fine there)
+                    const int cur = (h.lid + 1) % 3;
+                    uint32_t *lists[3] = {tails.p, front0.p, tails2.p};
+                    PADO_CUDA(cudaMemcpyAsync(lists[cur], retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
+                    h.tcnt[cur] = h.retry_cnt;
+                    h.hcnt[cur] = 0;
                 }
                 h.retry_cnt = 0;
                 h.status = 0;

@@ -155,7 +155,7 @@ __device__ void root_init_phase(const UnwDev &d, const uint32_t *roots, uint32_t
 // With gmap set, root r's row is (r - base) % B of its graph's block (batches
 // are B-aligned within a graph, so this is r - s of the batch r belongs to).
 __device__ void dm_rows_phase(const UnwDev &d, const uint32_t *roots, uint32_t nroots, uint32_t s, int fill,
-                              const GDesc *gd = nullptr, const uint16_t *gmap = nullptr)
+                              const GDesc *gd = nullptr, const uint16_t *gmap = nullptr, uint8_t *dm = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -168,7 +168,7 @@ __device__ void dm_rows_phase(const UnwDev &d, const uint32_t *roots, uint32_t n
             hb = x.base;
             row = d.dm + x.dm_off + (uint64_t)((r - hb) % d.B) * x.n;  // fields fixed for the launch
         } else {
-            row = d.dm + (uint64_t)(r - s) * d.n;
+            row = (dm ? dm : d.dm) + (uint64_t)(r - s) * d.n;
         }
         const uint64_t base = d.lab_off[r];
         const uint32_t len = d.lab_len[r];
@@ -366,6 +366,13 @@ struct PullArgs {
     const GDesc *gd = nullptr;       // many-graph labeling: per-graph state ...
     const uint16_t *gmap = nullptr;  // ... and the graph of each vertex
     GDesc *gd_mut = nullptr;         // the same array, for the per-graph counters
+    // Fused marking (persistent one-graph loop): a tail that gains labels marks
+    // its own tails for the next level right away (stamp next_stamp) instead of
+    // joining front_next for a separate mark phase.
+    uint32_t *next_tails = nullptr, *next_tails_cnt = nullptr;
+    uint32_t *next_htails = nullptr, *next_htails_cnt = nullptr;
+    uint32_t next_stamp = 0;
+    uint8_t *dm = nullptr;           // dist_matrix of the current batch (default d.dm)
 };
 
 // The batch a tail belongs to: roots [s, e), batch id b, level iter, and its
@@ -378,10 +385,40 @@ struct BatchCtx {
 
 __device__ __forceinline__ BatchCtx tail_ctx(const UnwDev &d, const PullArgs &a, uint32_t t)
 {
-    if (!a.gmap) return BatchCtx{a.s, a.e_roots, a.b, a.iter, 0u, d.n, d.dm, 0u};
+    if (!a.gmap) return BatchCtx{a.s, a.e_roots, a.b, a.iter, 0u, d.n, a.dm ? a.dm : d.dm, 0u};
     const uint32_t g = a.gmap[t];
     const GDesc &x = a.gd[g];
     return BatchCtx{gd_u32(x.s), gd_u32(x.e), gd_u32(x.b), gd_u32(x.iter), x.base, x.n, d.dm + x.dm_off, g};
+}
+
+// Marks the tails of head h for the level stamped `stamp`: neighbours t > mn
+// (descending list, so the scan stops at the first t <= mn) that are not BP
+// vertices, each once per level (tail stamp), into the light or heavy list.
+// A warp scans 32 entries per step; warp w of `nw` starts at chunk w.
+__device__ __forceinline__ void mark_tails(const UnwDev &d, uint32_t h, uint32_t mn, uint32_t stamp, uint32_t *tails,
+                                           uint32_t *tails_cnt, uint32_t *htails, uint32_t *htails_cnt, int lane,
+                                           uint32_t w, uint32_t nw, unsigned long long &bytes)
+{
+    const uint32_t e_end = d.off[h + 1];
+    for (uint32_t e0 = d.off[h] + 32 * w; e0 < e_end; e0 += 32 * nw) {
+        const uint32_t e = e0 + lane;
+        const bool in = e < e_end;
+        const uint32_t t = in ? d.adj[e] : 0u;
+        const bool ok = in && t > mn;
+        bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
+        bool appended = false;
+        if (ok && !d.used[t] && d.tail_stamp[t] != stamp) {
+            if (atomicExch(&d.tail_stamp[t], stamp) != stamp) {
+                if (d.off[t + 1] - d.off[t] >= HEAVY_DEG)
+                    htails[agg_append_by(htails_cnt, 1u)] = t;
+                else
+                    tails[agg_append_by(tails_cnt, 0u)] = t;
+                appended = true;
+            }
+        }
+        bytes += __popc(__ballot_sync(FULL, appended)) * 8ull;
+        if (__ballot_sync(FULL, in && !ok)) break;
+    }
 }
 
 // One heavy tail, processed by the whole block.
@@ -561,10 +598,13 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             d.last_cnt[cp][t] = nadd;
             d.last_min[cp][t] = hs.ctr[4];
             d.act_stamp[cp][t] = a.lid_cur;
-            a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
+            if (!a.next_tails) a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
             if (a.gd_mut) atomicAdd(&a.gd_mut[bc.g].fcnt[cp], 1u);
             bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0) + (hs.ctr[6] ? 10ull * len : 0);
         }
+        if (a.next_tails)
+            mark_tails(d, t, hs.ctr[4], a.next_stamp, a.next_tails, a.next_tails_cnt, a.next_htails,
+                       a.next_htails_cnt, lane, warp, blockDim.x >> 5, bytes);
     }
     for (uint32_t x = tid; x < d.words; x += blockDim.x) d.ind[(uint64_t)t * d.words + x] = hs.ind[x];
     if (tid == 0) d.ind_stamp[t] = bc.b + 1;
@@ -780,9 +820,12 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             d.last_cnt[cp][t] = nadd;
             d.last_min[cp][t] = mn;
             d.act_stamp[cp][t] = a.lid_cur;
-            a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
+            if (!a.next_tails) a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
             if (a.gd_mut) atomicAdd(&a.gd_mut[bc.g].fcnt[cp], 1u);
         }
+        if (a.next_tails)
+            mark_tails(d, t, mn, a.next_stamp, a.next_tails, a.next_tails_cnt, a.next_htails, a.next_htails_cnt, lane,
+                       0, 1, bytes);
     }
     for (uint32_t x = lane; x < d.words; x += 32) d.ind[(uint64_t)t * d.words + x] = wr.ind[x];
     if (lane == 0) d.ind_stamp[t] = bc.b + 1;
@@ -823,8 +866,15 @@ __device__ void pull_phase(const UnwDev &d, const PullArgs &a, unsigned char *pu
 constexpr unsigned long long BARRIER_TIMEOUT_NS = 4000000000ull;
 constexpr uint32_t ST_BARRIER_TIMEOUT = 8u;
 
+// Arrivals are counted per group of BAR_GROUP blocks (each group counter on
+// its own 128-byte line); the last arriver of a group bumps the top counter,
+// and the last group releases everyone by advancing `gen`.  That keeps the
+// serialised atomics on any one address to ~BAR_GROUP instead of the grid size.
+constexpr uint32_t BAR_GROUP = 32;
+constexpr uint32_t BAR_MAX_GROUPS = 64;   // grids up to 2048 blocks
 struct GridBar {
-    uint32_t arrive, gen;
+    uint32_t gen, top, pad[30];
+    uint32_t grp[BAR_MAX_GROUPS][32];
 };
 
 __device__ __forceinline__ uint32_t vload(const uint32_t *p) { return *(const volatile uint32_t *)p; }
@@ -845,16 +895,25 @@ __device__ bool grid_barrier(GridBar *bar, uint32_t *status)
         volatile uint32_t *gen = &bar->gen;
         const uint32_t g = *gen;
         __threadfence();
-        const uint32_t arrived = atomicAdd(&bar->arrive, 1u) + 1u;
+        const uint32_t grp = blockIdx.x / BAR_GROUP;
+        const uint32_t ngrp = (gridDim.x + BAR_GROUP - 1) / BAR_GROUP;
+        const uint32_t gsize = min(BAR_GROUP, gridDim.x - grp * BAR_GROUP);
         int good = 1;
-        if (arrived == gridDim.x) {
-            atomicExch(&bar->arrive, 0u);
+        bool last = false;
+        if (atomicAdd(&bar->grp[grp][0], 1u) + 1u == gsize) {
+            atomicExch(&bar->grp[grp][0], 0u);
+            if (atomicAdd(&bar->top, 1u) + 1u == ngrp) {
+                atomicExch(&bar->top, 0u);
+                last = true;
+            }
+        }
+        if (last) {
             __threadfence();
             atomicAdd(&bar->gen, 1u);
         } else {
             const unsigned long long t0 = gtimer();
             while (*gen == g) {
-                __nanosleep(32);
+                __nanosleep(20);
                 if (gtimer() - t0 > BARRIER_TIMEOUT_NS) {
                     atomicOr(status, ST_BARRIER_TIMEOUT);
                     good = 0;
