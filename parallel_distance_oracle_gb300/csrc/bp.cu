@@ -13,24 +13,27 @@
 //     edge (d -> d+1) ORs the parent's S^-1 / S^0 into the child's (:367-371).
 //   * stored row: (d, S^-1, S^0 & ~S^-1) (:377-381); an unused slot (no root
 //     left) stores d = 255 and empty sets (:288-292).
-// Device mapping: the BFS of up to GROUP roots run together, level by level,
-// over one combined frontier of (slot, vertex) entries, and every set update
-// is a PULL (an OR reduction over a vertex's own adjacency, stored by the one
-// thread that owns the vertex) instead of a per-edge atomic push:
-//   bp_level_kernel(d):  each v at level d ORs S^-1 of its level-d neighbours
-//       into S^0[v] (the sibling step) and claims its unreached neighbours for
-//       level d+1 (CAS on the level array; warp-aggregated appends);
-//   bp_parent_kernel(d): each u at level d+1 ORs S^-1 and S^0 of its level-d
-//       neighbours (its parents, whose S^0 the previous kernel finished) into
-//       its own sets (the child step).
-// The child step of the reference pushes parent sets along every d -> d+1
-// edge; pulling them over the same edges gives the same ORs.  Frontier
-// vertices of degree >= HEAVY are spread over every warp of the grid (partial
-// ORs combined with one atomicOr per warp); those of degree <= SMALL_DEG get
-// SUB lanes each (8 per warp: most vertices of sparse graphs); the rest get one
-// warp each.  OR is order-independent, so rows are bit-identical.  Per root
-// the adjacency of every reached vertex is streamed twice with a 4 B level
-// lookup per edge; per-vertex state is 20 B.
+//
+// Device mapping: all K <= 64 BFSes run together, level by level, over the
+// final vertex-major rows (bpd[v][K], bps[v][K]) -- a multi-source BFS.  Per
+// vertex a 64-bit mask says which slots have reached it, and a level-stamped
+// mask which slots have it on the current level.  A warp works on one vertex
+// with lane i owning slots i and i + 32, so a neighbour's row is read with
+// one coalesced 16-byte load per lane and only for the slots where it matters;
+// the adjacency of a vertex is scanned once per level for all slots together
+// instead of once per slot.  Per level d:
+//   bp_sibling_kernel: each vertex v on level d (in any slot) ORs S^-1 of its
+//       neighbours that share a level-d slot into S^0[v] (the sibling step),
+//       and lists the neighbours that still miss a slot v has on level d;
+//   bp_child_kernel: each listed vertex w takes, per slot it has not reached,
+//       the OR of S^-1 / S^0 over its neighbours on level d in that slot (the
+//       child step); slots so reached get level d+1 and put w on level d+1.
+// The child step pulls along the same edges the reference pushes along, and
+// every update is an OR, so the rows are bit-identical.  Vertices of degree
+// >= HEAVY are worked on by a whole block (8 warps over the neighbours, one
+// shared-memory reduction).  For many graphs in one union id space, slot i
+// holds every graph's i-th root: the graphs are disjoint, so their BFSes
+// never meet.
 
 #include <algorithm>
 
@@ -39,230 +42,264 @@
 namespace pado {
 namespace {
 
-constexpr uint32_t LV_INF = 255u;
-constexpr uint32_t GROUP = 16;       // BP roots labeled concurrently
-constexpr uint32_t HEAVY = 4096;     // frontier vertices split over all warps
-constexpr uint32_t SMALL_DEG = 16;   // frontier vertices up to this degree share a warp ...
-constexpr uint32_t SUB = 4;          // ... SUB lanes each
+constexpr unsigned FULL_MASK = 0xffffffffu;
+constexpr uint32_t HEAVY = 2048;     // vertices worked on by a whole block
+constexpr int BP_THREADS = 256;
+constexpr int BP_WARPS = BP_THREADS / 32;
 
-enum FrontClass : int { FC_LIGHT = 0, FC_HEAVY = 1, FC_SMALL = 2 };
+// Slots where a vertex is on level `lvl`; valid only if `lvl` matches the level
+// being read (the two parity buffers are never cleared).
+struct LevelMask {
+    unsigned long long bits;
+    unsigned long long lvl;
+};
 
-__host__ __device__ __forceinline__ int front_class(uint32_t deg)
-{
-    return deg >= HEAVY ? FC_HEAVY : (deg <= SMALL_DEG ? FC_SMALL : FC_LIGHT);
-}
-
-__device__ __forceinline__ uint64_t warp_or64(uint64_t v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v |= __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-struct BpState {
-    uint32_t n;
-    uint32_t slots;
+struct MsState {
+    uint32_t n, K;
     const uint32_t *off;
     const uint32_t *adj;
-    uint32_t *lvl;   // [slots][n], LV_INF = unreached
-    uint64_t *sm1;   // [slots][n]
-    uint64_t *s0;    // [slots][n]
+    uint8_t *bpd;          // [n][K]: level per slot, 255 = unreached (final rows)
+    ulonglong2 *bps;       // [n][K]: (S^-1, S^0); S^0 is masked by ~S^-1 at the end
+    unsigned long long *reach;  // [n]: slots that have reached v
+    LevelMask *lm[2];      // [n]: slots with v on level d, in lm[d & 1]
+    uint32_t *cstamp;      // [n]: candidate stamp (level + 1)
+    uint32_t *fstamp;      // [n]: frontier stamp (level)
     unsigned long long *work;
 };
 
-// Frontier entry: slot << 32 | vertex.
-__device__ __forceinline__ uint32_t ent_slot(uint64_t e) { return (uint32_t)(e >> 32); }
-__device__ __forceinline__ uint32_t ent_v(uint64_t e) { return (uint32_t)e; }
-
-// A frontier: entry lists by class (FC_*), with their counts.
-struct Front {
-    const uint64_t *list[3];
-    const uint32_t *cnt;  // cnt[FC_*]
-};
-struct NextFront {
-    uint64_t *list[3];
-    uint32_t *cnt;
+// A list of vertices split by degree: light (a warp each) and heavy (a block each).
+struct VList {
+    uint32_t *light, *heavy;
+    uint32_t *cnt;         // cnt[0] light, cnt[1] heavy
 };
 
-__global__ void bp_reset_kernel(BpState st)
+__device__ __forceinline__ unsigned long long level_bits(const MsState &st, uint32_t v, uint32_t d)
 {
-    const uint64_t tot = (uint64_t)st.slots * st.n;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tot; i += (uint64_t)gridDim.x * blockDim.x) {
-        st.lvl[i] = LV_INF;
-        st.sm1[i] = 0;
-        st.s0[i] = 0;
-    }
+    const LevelMask m = st.lm[d & 1][v];
+    return m.lvl == d ? m.bits : 0ull;
 }
 
-// seeds: (slot, vertex, level, S^-1) for each root and its selected neighbours.
-__global__ void bp_seed_kernel(BpState st, const uint32_t *sslot, const uint32_t *sv, const uint32_t *slv,
-                               const uint64_t *sbits, uint32_t cnt)
+__device__ __forceinline__ void vlist_append(const MsState &st, const VList &l, uint32_t v)
 {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < cnt) {
-        const uint64_t k = (uint64_t)sslot[i] * st.n + sv[i];
-        st.lvl[k] = slv[i];
-        st.sm1[k] = sbits[i];
-    }
+    const bool heavy = st.off[v + 1] - st.off[v] >= HEAVY;
+    if (heavy)
+        l.heavy[agg_append_by(&l.cnt[1], 1u)] = v;
+    else
+        l.light[agg_append_by(&l.cnt[0], 0u)] = v;
 }
 
-// Per-entry accumulator of the two pull kernels.
-struct BpAcc {
-    uint64_t a = 0, b = 0;
-    uint32_t hits = 0;
-};
-
-// Runs `edge(so, slot, v, tv, acc)` over the adjacency of every frontier entry
-// and `fin(so, v, acc, atomic)` once per entry with the entry's OR-reduced
-// accumulator (atomic: several warps share the entry, combine with atomicOr).
-template <class Edge, class Fin>
-__device__ __forceinline__ void bp_pull(const BpState &st, const Front &f, unsigned long long &bytes, Edge edge, Fin fin)
+// Sibling step for frontier vertex v over the neighbour range handled by this
+// warp (chunks w, w + nw, ...); returns the per-lane ORs (slots lane, lane+32).
+__device__ __forceinline__ void sibling_range(const MsState &st, uint32_t v, unsigned long long fv, uint32_t d,
+                                              uint32_t w, uint32_t nw, const VList &cand, unsigned long long &acc0,
+                                              unsigned long long &acc1, unsigned long long &bytes)
 {
     const int lane = threadIdx.x & 31;
+    const uint32_t e_end = st.off[v + 1];
+    for (uint32_t e0 = st.off[v] + 32 * w; e0 < e_end; e0 += 32 * nw) {
+        const uint32_t e = e0 + lane;
+        const bool in = e < e_end;
+        const uint32_t u = in ? st.adj[e] : 0u;
+        const unsigned long long fu = in ? level_bits(st, u, d) : 0ull;
+        const unsigned long long ru = in ? st.reach[u] : ~0ull;
+        // u misses a slot v has on level d: it may be reached at d+1
+        if (in && (fv & ~ru) && st.cstamp[u] != d + 1 && atomicExch(&st.cstamp[u], d + 1) != d + 1)
+            vlist_append(st, cand, u);
+        unsigned long long common = fv & fu;
+        uint32_t mask = __ballot_sync(FULL_MASK, common != 0);
+        bytes += 20ull * __popc(__ballot_sync(FULL_MASK, in));
+        while (mask) {
+            const int k = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const uint32_t uk = __shfl_sync(FULL_MASK, u, k);
+            const unsigned long long ck = __shfl_sync(FULL_MASK, common, k);
+            if ((ck >> lane) & 1ull) acc0 |= st.bps[(uint64_t)uk * st.K + lane].x;
+            if ((ck >> (lane + 32)) & 1ull) acc1 |= st.bps[(uint64_t)uk * st.K + lane + 32].x;
+            bytes += 8ull * __popcll(ck);
+        }
+    }
+}
+
+// Child step for candidate w over this warp's neighbour chunks: per lane, the
+// ORs of S^-1 / S^0 of level-d neighbours in the slots w has not reached, and
+// the mask of slots so reached.
+__device__ __forceinline__ void child_range(const MsState &st, uint32_t w, unsigned long long rw, uint32_t d,
+                                            uint32_t wi, uint32_t nw, unsigned long long &newm, ulonglong2 &a0,
+                                            ulonglong2 &a1, unsigned long long &bytes)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t e_end = st.off[w + 1];
+    for (uint32_t e0 = st.off[w] + 32 * wi; e0 < e_end; e0 += 32 * nw) {
+        const uint32_t e = e0 + lane;
+        const bool in = e < e_end;
+        const uint32_t u = in ? st.adj[e] : 0u;
+        const unsigned long long m = in ? (level_bits(st, u, d) & ~rw) : 0ull;
+        uint32_t mask = __ballot_sync(FULL_MASK, m != 0);
+        bytes += 20ull * __popc(__ballot_sync(FULL_MASK, in));
+        while (mask) {
+            const int k = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const uint32_t uk = __shfl_sync(FULL_MASK, u, k);
+            const unsigned long long mk = __shfl_sync(FULL_MASK, m, k);
+            newm |= mk;
+            if ((mk >> lane) & 1ull) {
+                const ulonglong2 x = st.bps[(uint64_t)uk * st.K + lane];
+                a0.x |= x.x;
+                a0.y |= x.y;
+            }
+            if ((mk >> (lane + 32)) & 1ull) {
+                const ulonglong2 x = st.bps[(uint64_t)uk * st.K + lane + 32];
+                a1.x |= x.x;
+                a1.y |= x.y;
+            }
+            bytes += 16ull * __popcll(mk);
+        }
+    }
+}
+
+// Commit of the child step for w by one warp: levels, sets, masks, frontier.
+__device__ __forceinline__ void child_commit(const MsState &st, uint32_t w, unsigned long long rw,
+                                             unsigned long long newm, ulonglong2 a0, ulonglong2 a1, uint32_t d,
+                                             const VList &next)
+{
+    const int lane = threadIdx.x & 31;
+    if (!newm) return;
+    const uint64_t row = (uint64_t)w * st.K;
+    if ((newm >> lane) & 1ull) {
+        st.bpd[row + lane] = (uint8_t)(d + 1);
+        ulonglong2 x = st.bps[row + lane];
+        x.x |= a0.x;
+        x.y |= a0.y;
+        st.bps[row + lane] = x;
+    }
+    if ((newm >> (lane + 32)) & 1ull) {
+        st.bpd[row + lane + 32] = (uint8_t)(d + 1);
+        ulonglong2 x = st.bps[row + lane + 32];
+        x.x |= a1.x;
+        x.y |= a1.y;
+        st.bps[row + lane + 32] = x;
+    }
+    if (lane == 0) {
+        st.reach[w] = rw | newm;
+        LevelMask &nm = st.lm[(d + 1) & 1][w];
+        const unsigned long long prev = nm.lvl == d + 1 ? nm.bits : 0ull;  // level-1 seeds are there already
+        nm.bits = prev | newm;
+        nm.lvl = d + 1;
+        if (atomicExch(&st.fstamp[w], d + 1) != d + 1) vlist_append(st, next, w);
+    }
+}
+
+__device__ __forceinline__ void block_or(unsigned long long *sm, unsigned long long &v, int lane, int warp)
+{
+    sm[warp * 32 + lane] = v;
+    __syncthreads();
+    if (warp == 0) {
+        for (int k = 1; k < BP_WARPS; ++k) v |= sm[k * 32 + lane];
+    }
+    __syncthreads();
+}
+
+// Level d, sibling step over the frontier (heavy vertices by blocks, then
+// light ones by warps); also lists the child candidates of level d.
+__global__ void __launch_bounds__(BP_THREADS) bp_sibling_kernel(MsState st, VList front, uint32_t d, VList cand)
+{
+    __shared__ unsigned long long sm[BP_WARPS * 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long bytes = 0;
+    const uint32_t hc = front.cnt[1];
+    for (uint32_t q = blockIdx.x; q < hc; q += gridDim.x) {
+        const uint32_t v = front.heavy[q];
+        const unsigned long long fv = level_bits(st, v, d);
+        unsigned long long a0 = 0, a1 = 0;
+        sibling_range(st, v, fv, d, warp, BP_WARPS, cand, a0, a1, bytes);
+        block_or(sm, a0, lane, warp);
+        block_or(sm, a1, lane, warp);
+        if (warp == 0) {
+            const uint64_t row = (uint64_t)v * st.K;
+            if (a0 && lane < (int)st.K) st.bps[row + lane].y |= a0;
+            if (a1 && lane + 32 < (int)st.K) st.bps[row + lane + 32].y |= a1;
+        }
+    }
+    const uint32_t lc = front.cnt[0];
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    // heavy vertices: every warp takes 32-edge chunks of each
-    const uint32_t hc = f.cnt[FC_HEAVY];
-    for (uint32_t q = 0; q < hc; ++q) {
-        const uint64_t ent = f.list[FC_HEAVY][q];
-        const uint32_t slot = ent_slot(ent), v = ent_v(ent);
-        const uint64_t so = (uint64_t)slot * st.n;
-        const uint32_t e_end = st.off[v + 1];
-        BpAcc acc;
-        for (uint32_t e = st.off[v] + gw * 32 + lane; e < e_end; e += nw * 32) edge(so, slot, v, st.adj[e], acc);
-        acc.a = warp_or64(acc.a);
-        acc.b = warp_or64(acc.b);
-        if (lane == 0) fin(so, v, acc, true);
-        if (lane == 0 && gw == 0) bytes += 20 + 8ull * (e_end - st.off[v]);
-        bytes += 8ull * acc.hits;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < lc; q += nw) {
+        const uint32_t v = front.light[q];
+        const unsigned long long fv = level_bits(st, v, d);
+        unsigned long long a0 = 0, a1 = 0;
+        sibling_range(st, v, fv, d, 0, 1, cand, a0, a1, bytes);
+        const uint64_t row = (uint64_t)v * st.K;
+        if (a0 && lane < (int)st.K) st.bps[row + lane].y |= a0;
+        if (a1 && lane + 32 < (int)st.K) st.bps[row + lane + 32].y |= a1;
     }
-    // light vertices: a warp each
-    const uint32_t lc = f.cnt[FC_LIGHT];
-    for (uint32_t q = gw; q < lc; q += nw) {
-        const uint64_t ent = f.list[FC_LIGHT][q];
-        const uint32_t slot = ent_slot(ent), v = ent_v(ent);
-        const uint64_t so = (uint64_t)slot * st.n;
-        const uint32_t e_end = st.off[v + 1];
-        BpAcc acc;
-        for (uint32_t e = st.off[v] + lane; e < e_end; e += 32) edge(so, slot, v, st.adj[e], acc);
-        acc.a = warp_or64(acc.a);
-        acc.b = warp_or64(acc.b);
-        if (lane == 0) {
-            fin(so, v, acc, false);
-            bytes += 20 + 8ull * (e_end - st.off[v]);
-        }
-        bytes += 8ull * acc.hits;
-    }
-    // small vertices: SUB lanes each, 32 / SUB per warp (warp-uniform loop)
-    const uint32_t sc = f.cnt[FC_SMALL];
-    const uint32_t per = 32 / SUB, sub = lane % SUB;
-    for (uint64_t qb = (uint64_t)gw * per; qb < sc; qb += (uint64_t)nw * per) {
-        const uint64_t q = qb + lane / SUB;
-        BpAcc acc;
-        uint64_t so = 0;
-        uint32_t v = 0;
-        if (q < sc) {
-            const uint64_t ent = f.list[FC_SMALL][q];
-            const uint32_t slot = ent_slot(ent);
-            v = ent_v(ent);
-            so = (uint64_t)slot * st.n;
-            const uint32_t e_end = st.off[v + 1];
-            for (uint32_t e = st.off[v] + sub; e < e_end; e += SUB) edge(so, slot, v, st.adj[e], acc);
-            if (sub == 0) bytes += 20 + 8ull * (e_end - st.off[v]);
-        }
-#pragma unroll
-        for (int o = 1; o < (int)SUB; o <<= 1) {
-            acc.a |= __shfl_xor_sync(0xffffffffu, acc.a, o);
-            acc.b |= __shfl_xor_sync(0xffffffffu, acc.b, o);
-        }
-        if (q < sc && sub == 0) fin(so, v, acc, false);
-        bytes += 8ull * acc.hits;
-    }
+    if (st.work && lane == 0 && bytes) atomicAdd(&st.work[W_BP_SIB], bytes);
 }
 
-// Level d: the sibling step (S^0[v] |= S^-1[tv], tv at level d) and the
-// discovery of level d+1 (pado_unw_unv_unp.h:362-371).
-__global__ void __launch_bounds__(256, 4) bp_level_kernel(BpState st, Front f, uint32_t d, NextFront nx,
-                                                          uint32_t *status)
+// Level d, child step over the candidates; builds the frontier of level d+1.
+__global__ void __launch_bounds__(BP_THREADS) bp_child_kernel(MsState st, VList cand, uint32_t d, VList next,
+                                                              uint32_t *status)
 {
+    __shared__ unsigned long long sm[BP_WARPS * 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long bytes = 0;
-    bp_pull(
-        st, f, bytes,
-        [&](uint64_t so, uint32_t slot, uint32_t, uint32_t tv, BpAcc &acc) {
-            const uint32_t l = st.lvl[so + tv];
-            if (l == d) {
-                acc.a |= st.sm1[so + tv];
-                ++acc.hits;
-            } else if (l == LV_INF) {
-                if (d + 1 >= LV_INF) {
-                    atomicOr(status, ST_LEVEL_OVERFLOW);
-                } else if (atomicCAS(&st.lvl[so + tv], LV_INF, d + 1) == LV_INF) {
-                    const int c = front_class(st.off[tv + 1] - st.off[tv]);
-                    nx.list[c][agg_append_by(&nx.cnt[c], (unsigned)c)] = ((uint64_t)slot << 32) | tv;
-                    acc.hits += 2;
-                }
-            }
-        },
-        [&](uint64_t so, uint32_t v, const BpAcc &acc, bool atomic) {
-            if (!acc.a) return;
-            if (atomic)
-                atomicOr((unsigned long long *)&st.s0[so + v], (unsigned long long)acc.a);
-            else
-                st.s0[so + v] |= acc.a;
-        });
-    if (st.work && bytes) atomicAdd(&st.work[W_BP_SIB], bytes);
+    if (d + 1 >= U8_INF) {
+        if ((cand.cnt[0] || cand.cnt[1]) && threadIdx.x == 0 && blockIdx.x == 0) atomicOr(status, ST_LEVEL_OVERFLOW);
+        return;
+    }
+    const uint32_t hc = cand.cnt[1];
+    for (uint32_t q = blockIdx.x; q < hc; q += gridDim.x) {
+        const uint32_t w = cand.heavy[q];
+        const unsigned long long rw = st.reach[w];
+        unsigned long long newm = 0;
+        ulonglong2 a0 = make_ulonglong2(0, 0), a1 = make_ulonglong2(0, 0);
+        child_range(st, w, rw, d, warp, BP_WARPS, newm, a0, a1, bytes);
+        block_or(sm, newm, lane, warp);
+        block_or(sm, a0.x, lane, warp);
+        block_or(sm, a0.y, lane, warp);
+        block_or(sm, a1.x, lane, warp);
+        block_or(sm, a1.y, lane, warp);
+        if (warp == 0) child_commit(st, w, rw, newm, a0, a1, d, next);  // newm is the same in every lane
+    }
+    const uint32_t lc = cand.cnt[0];
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < lc; q += nw) {
+        const uint32_t w = cand.light[q];
+        const unsigned long long rw = st.reach[w];
+        unsigned long long newm = 0;
+        ulonglong2 a0 = make_ulonglong2(0, 0), a1 = make_ulonglong2(0, 0);
+        child_range(st, w, rw, d, 0, 1, newm, a0, a1, bytes);
+        child_commit(st, w, rw, newm, a0, a1, d, next);
+    }
+    if (st.work && lane == 0 && bytes) atomicAdd(&st.work[W_BP_CHILD], bytes);
 }
 
-// The child step for the vertices first reached at level d+1: OR the sets of
-// their level-d neighbours (pado_unw_unv_unp.h:367-371).
-__global__ void __launch_bounds__(256, 4) bp_parent_kernel(BpState st, Front f, uint32_t d)
+__global__ void bp_init_kernel(LevelMask *a, LevelMask *b, uint32_t n)
 {
-    unsigned long long bytes = 0;
-    bp_pull(
-        st, f, bytes,
-        [&](uint64_t so, uint32_t, uint32_t, uint32_t p, BpAcc &acc) {
-            if (st.lvl[so + p] == d) {
-                acc.a |= st.sm1[so + p];
-                acc.b |= st.s0[so + p];
-                acc.hits += 2;
-            }
-        },
-        [&](uint64_t so, uint32_t u, const BpAcc &acc, bool atomic) {
-            if (atomic) {
-                if (acc.a) atomicOr((unsigned long long *)&st.sm1[so + u], (unsigned long long)acc.a);
-                if (acc.b) atomicOr((unsigned long long *)&st.s0[so + u], (unsigned long long)acc.b);
-            } else {
-                if (acc.a) st.sm1[so + u] |= acc.a;
-                if (acc.b) st.s0[so + u] |= acc.b;
-            }
-        });
-    if (st.work && bytes) atomicAdd(&st.work[W_BP_CHILD], bytes);
-}
-
-// Rows of slots [0, slots) into BP columns [i0, i0 + slots).
-__global__ void bp_store_kernel(BpState st, uint32_t K, uint32_t i0, uint8_t *bpd, uint64_t *bps)
-{
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < st.n; v += gridDim.x * blockDim.x) {
-        for (uint32_t j = 0; j < st.slots; ++j) {
-            const uint64_t k = (uint64_t)j * st.n + v;
-            const uint64_t a = st.sm1[k];
-            bpd[(uint64_t)v * K + i0 + j] = (uint8_t)st.lvl[k];
-            bps[((uint64_t)v * K + i0 + j) * 2] = a;
-            bps[((uint64_t)v * K + i0 + j) * 2 + 1] = st.s0[k] & ~a;
-        }
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        a[v] = LevelMask{0ull, ~0ull};
+        b[v] = LevelMask{0ull, ~0ull};
     }
 }
 
-__global__ void bp_empty_slots_kernel(uint32_t n, uint32_t K, uint32_t i0, uint8_t *bpd, uint64_t *bps)
+// Seeds: (slot, vertex, level, S^-1) for each root and its selected neighbours.
+__global__ void bp_seed_kernel(MsState st, const uint32_t *sslot, const uint32_t *sv, const uint32_t *slv,
+                               const uint64_t *sbits, uint32_t cnt)
 {
-    const uint32_t w = K - i0;
-    for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < (uint64_t)n * w;
-         x += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t v = x / w, i = i0 + x % w;
-        bpd[v * K + i] = U8_INF;
-        bps[(v * K + i) * 2] = 0;
-        bps[(v * K + i) * 2 + 1] = 0;
-    }
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt) return;
+    const uint32_t v = sv[i], slot = sslot[i], l = slv[i];
+    st.bpd[(uint64_t)v * st.K + slot] = (uint8_t)l;
+    st.bps[(uint64_t)v * st.K + slot].x = sbits[i];
+    atomicOr(&st.reach[v], 1ull << slot);
+    atomicOr(&st.lm[l & 1][v].bits, 1ull << slot);
+    st.lm[l & 1][v].lvl = l;
+    if (l == 1) st.fstamp[v] = 1;
+}
+
+__global__ void bp_finish_kernel(MsState st)
+{
+    const uint64_t tot = (uint64_t)st.n * st.K;
+    for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < tot; x += (uint64_t)gridDim.x * blockDim.x)
+        st.bps[x].y &= ~st.bps[x].x;
 }
 
 }  // namespace
@@ -305,105 +342,116 @@ BpResult bp_run(const HostGraph &hg, const DevGraph &g, uint32_t K, const std::v
     BpResult res;
     const uint32_t n = hg.n;
     if (K == 0 || n == 0) return res;
-    // slots [0, nroots) have a root in at least one graph; a graph with fewer
-    // roots gets unreached (255, empty) rows in its remaining slots, which is
-    // what the reference stores for a slot without a root (:288-292).
-    uint32_t nroots = 0;
-    while (nroots < std::min<size_t>(K, seeds.size()) && !seeds[nroots].empty()) ++nroots;
-
-    const uint32_t gsize = std::min<uint32_t>(GROUP, std::max<uint32_t>(nroots, 1));
-    DBuf<uint32_t> lvl((uint64_t)gsize * n), cnts(8), status(1);
-    DBuf<uint64_t> sm1((uint64_t)gsize * n), s0((uint64_t)gsize * n);
-    // frontier lists by class, double-buffered: fr[buffer][class]
-    DBuf<uint64_t> fr[2][3];
-    for (auto &side : fr)
-        for (auto &l : side) l.alloc((uint64_t)gsize * n);
-    size_t max_seeds = 1;
-    for (uint32_t i = 0; i < nroots; i += gsize) {
-        size_t c = 0;
-        for (uint32_t j = i; j < std::min(nroots, i + gsize); ++j) c += seeds[j].size();
-        max_seeds = std::max(max_seeds, c);
-    }
-    DBuf<uint32_t> seed_slot(max_seeds), seed_v(max_seeds), seed_l(max_seeds);
-    DBuf<uint64_t> seed_b(max_seeds);
-    status.fill_bytes(0, s);
-    uint32_t *h_cnt = nullptr;
-    PADO_CUDA(cudaMallocHost((void **)&h_cnt, 8 * sizeof(uint32_t)));
+    PADO_CHECK(K <= MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
     cudaEvent_t e0, e1;
     PADO_CUDA(cudaEventCreate(&e0));
     PADO_CUDA(cudaEventCreate(&e1));
-    PADO_CUDA(cudaEventRecord(e0, s));
-    const unsigned vb = 256;
-    const unsigned level_grid = 152u * 8u;
+    uint32_t *h_cnt = nullptr;
     try {
-        for (uint32_t g0 = 0; g0 < nroots; g0 += gsize) {
-            const uint32_t slots = std::min(gsize, nroots - g0);
-            BpState st{n, slots, g.off.p, g.adj.p, lvl.p, sm1.p, s0.p, work_counters()};
-            PADO_LAUNCH("bp_reset_kernel", s, bp_reset_kernel<<<grid_for((uint64_t)slots * n, vb), vb, 0, s>>>(st));
-            std::vector<uint32_t> ss, sv, sl;
-            std::vector<uint64_t> sb, f0[3], f1[3];
-            for (uint32_t j = 0; j < slots; ++j) {
-                for (const BpSeed &x : seeds[g0 + j]) {
-                    ss.push_back(j);
-                    sv.push_back(x.v);
-                    sl.push_back(x.lvl);
-                    sb.push_back(x.bits);
-                    const uint64_t ent = ((uint64_t)j << 32) | x.v;
-                    const int c = front_class(hg.off[x.v + 1] - hg.off[x.v]);
-                    (x.lvl == 0 ? f0 : f1)[c].push_back(ent);
+        PADO_CUDA(cudaMallocHost((void **)&h_cnt, 8 * sizeof(uint32_t)));
+        PADO_CUDA(cudaEventRecord(e0, s));
+        // rows start unreached: level 255, empty sets (also the rows of slots no graph has a root for)
+        PADO_CUDA(cudaMemsetAsync(d_bpd, 0xff, (uint64_t)n * K, s));
+        PADO_CUDA(cudaMemsetAsync(d_bps, 0, (uint64_t)n * K * 16, s));
+        DBuf<unsigned long long> reach(n);
+        DBuf<LevelMask> lm0(n), lm1(n);
+        DBuf<uint32_t> cstamp(n), fstamp(n), cnts(8), status(1);
+        DBuf<uint32_t> fl[2], fh[2], cl, ch;
+        for (int i = 0; i < 2; ++i) {
+            fl[i].alloc(n);
+            fh[i].alloc(n);
+        }
+        cl.alloc(n);
+        ch.alloc(n);
+        reach.fill_bytes(0, s);
+        // empty masks stamped with a level no BFS reaches
+        PADO_LAUNCH("bp_init_kernel", s, bp_init_kernel<<<grid_for(n, 256), 256, 0, s>>>(lm0.p, lm1.p, n));
+        cstamp.fill_bytes(0, s);
+        fstamp.fill_bytes(0xff, s);
+        status.fill_bytes(0, s);
+        cnts.fill_bytes(0, s);
+        MsState st{n, K, g.off.p, g.adj.p, d_bpd, reinterpret_cast<ulonglong2 *>(d_bps), reach.p,
+                   {lm0.p, lm1.p}, cstamp.p, fstamp.p, work_counters()};
+
+        // seeds and the frontiers of levels 0 (roots) and 1 (selected neighbours), deduplicated
+        std::vector<uint32_t> ss, sv, sl;
+        std::vector<uint64_t> sb;
+        std::vector<uint32_t> f0[2], f1[2];
+        std::vector<uint8_t> in0(n, 0), in1(n, 0);
+        for (uint32_t j = 0; j < std::min<size_t>(K, seeds.size()); ++j) {
+            for (const BpSeed &x : seeds[j]) {
+                ss.push_back(j);
+                sv.push_back(x.v);
+                sl.push_back(x.lvl);
+                sb.push_back(x.bits);
+                const bool heavy = hg.off[x.v + 1] - hg.off[x.v] >= HEAVY;
+                if (x.lvl == 0 && !in0[x.v]) {
+                    in0[x.v] = 1;
+                    f0[heavy].push_back(x.v);
+                } else if (x.lvl == 1 && !in1[x.v]) {
+                    in1[x.v] = 1;
+                    f1[heavy].push_back(x.v);
                 }
             }
-            seed_slot.upload(ss.data(), ss.size(), s);
-            seed_v.upload(sv.data(), sv.size(), s);
-            seed_l.upload(sl.data(), sl.size(), s);
-            seed_b.upload(sb.data(), sb.size(), s);
-            PADO_LAUNCH("bp_seed_kernel", s,
-                        bp_seed_kernel<<<grid_for(sv.size(), 128), 128, 0, s>>>(st, seed_slot.p, seed_v.p, seed_l.p,
-                                                                              seed_b.p, (uint32_t)sv.size()));
-            // frontier 0 = the roots; frontier 1 starts with the selected neighbours
-            uint32_t init_cnt[8] = {};
-            for (int c = 0; c < 3; ++c) {
-                fr[0][c].upload(f0[c].data(), f0[c].size(), s);
-                fr[1][c].upload(f1[c].data(), f1[c].size(), s);
-                init_cnt[c] = (uint32_t)f0[c].size();
-                init_cnt[4 + c] = (uint32_t)f1[c].size();
-            }
-            PADO_CUDA(cudaMemcpyAsync(cnts.p, init_cnt, sizeof(init_cnt), cudaMemcpyHostToDevice, s));
-            int cur = 0;  // fr[cur] / counts cnts[4*cur ..] hold level d
-            uint32_t fsize = (uint32_t)(f0[0].size() + f0[1].size() + f0[2].size());
-            for (uint32_t d = 0; fsize > 0; ++d) {
-                uint32_t *cc = cnts.p + 4 * cur, *nc = cnts.p + 4 * (cur ^ 1);
-                Front f{{fr[cur][0].p, fr[cur][1].p, fr[cur][2].p}, cc};
-                NextFront nx{{fr[cur ^ 1][0].p, fr[cur ^ 1][1].p, fr[cur ^ 1][2].p}, nc};
-                PADO_LAUNCH("bp_level_kernel", s,
-                            bp_level_kernel<<<level_grid, 256, 0, s>>>(st, f, d, nx, status.p));
-                // the next frontier, complete now, pulls its parents' sets
-                const Front fn{{nx.list[0], nx.list[1], nx.list[2]}, nc};
-                PADO_LAUNCH("bp_parent_kernel", s, bp_parent_kernel<<<level_grid, 256, 0, s>>>(st, fn, d));
-                ++res.levels;
-                PADO_CUDA(cudaMemcpyAsync(h_cnt, nc, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-                PADO_CUDA(cudaMemcpyAsync(h_cnt + 3, status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-                PADO_CUDA(cudaMemsetAsync(cc, 0, 3 * sizeof(uint32_t), s));
-                PADO_CUDA(cudaStreamSynchronize(s));
-                if (h_cnt[3] & ST_LEVEL_OVERFLOW)
-                    throw Error(PADO_E_OVERFLOW, "bit-parallel BFS reached level 255 (uint8 distance overflow)");
-                fsize = h_cnt[0] + h_cnt[1] + h_cnt[2];
-                cur ^= 1;
-            }
-            PADO_LAUNCH("bp_store_kernel", s,
-                        bp_store_kernel<<<grid_for(n, vb), vb, 0, s>>>(st, K, g0, d_bpd, d_bps));
         }
-        if (nroots < K)
-            PADO_LAUNCH("bp_empty_slots_kernel", s,
-                        bp_empty_slots_kernel<<<grid_for((uint64_t)n * (K - nroots), vb), vb, 0, s>>>(n, K, nroots, d_bpd,
-                                                                                                      d_bps));
+        if (sv.empty()) {
+            PADO_CUDA(cudaEventRecord(e1, s));
+            PADO_CUDA(cudaEventSynchronize(e1));
+            PADO_CUDA(cudaEventElapsedTime(&res.ms, e0, e1));
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            cudaFreeHost(h_cnt);
+            return res;
+        }
+        DBuf<uint32_t> d_ss(ss.size()), d_sv(sv.size()), d_sl(sl.size());
+        DBuf<uint64_t> d_sb(sb.size());
+        d_ss.upload(ss.data(), ss.size(), s);
+        d_sv.upload(sv.data(), sv.size(), s);
+        d_sl.upload(sl.data(), sl.size(), s);
+        d_sb.upload(sb.data(), sb.size(), s);
+        PADO_LAUNCH("bp_seed_kernel", s,
+                    bp_seed_kernel<<<grid_for(sv.size(), 128), 128, 0, s>>>(st, d_ss.p, d_sv.p, d_sl.p, d_sb.p,
+                                                                          (uint32_t)sv.size()));
+        fl[0].upload(f0[0].data(), f0[0].size(), s);
+        fh[0].upload(f0[1].data(), f0[1].size(), s);
+        fl[1].upload(f1[0].data(), f1[0].size(), s);
+        fh[1].upload(f1[1].data(), f1[1].size(), s);
+        // cnts: [0,1] frontier d (light, heavy), [2,3] frontier d+1, [4,5] candidates
+        uint32_t init_cnt[8] = {(uint32_t)f0[0].size(), (uint32_t)f0[1].size(), (uint32_t)f1[0].size(),
+                                (uint32_t)f1[1].size(), 0, 0, 0, 0};
+        PADO_CUDA(cudaMemcpyAsync(cnts.p, init_cnt, sizeof(init_cnt), cudaMemcpyHostToDevice, s));
+        const unsigned grid = 152u * 8u;
+        int cur = 0;
+        uint32_t *ccur = cnts.p, *cnxt = cnts.p + 2, *ccand = cnts.p + 4;
+        uint32_t fsize = (uint32_t)(f0[0].size() + f0[1].size());
+        for (uint32_t d = 0; fsize > 0; ++d) {
+            const VList front{fl[cur].p, fh[cur].p, ccur};
+            const VList next{fl[cur ^ 1].p, fh[cur ^ 1].p, cnxt};
+            const VList cand{cl.p, ch.p, ccand};
+            PADO_LAUNCH("bp_sibling_kernel", s, bp_sibling_kernel<<<grid, BP_THREADS, 0, s>>>(st, front, d, cand));
+            PADO_LAUNCH("bp_child_kernel", s,
+                        bp_child_kernel<<<grid, BP_THREADS, 0, s>>>(st, cand, d, next, status.p));
+            ++res.levels;
+            PADO_CUDA(cudaMemcpyAsync(h_cnt, cnxt, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            PADO_CUDA(cudaMemcpyAsync(h_cnt + 2, status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            PADO_CUDA(cudaMemsetAsync(ccur, 0, 2 * sizeof(uint32_t), s));
+            PADO_CUDA(cudaMemsetAsync(ccand, 0, 2 * sizeof(uint32_t), s));
+            PADO_CUDA(cudaStreamSynchronize(s));
+            if (h_cnt[2] & ST_LEVEL_OVERFLOW)
+                throw Error(PADO_E_OVERFLOW, "bit-parallel BFS reached level 255 (uint8 distance overflow)");
+            fsize = h_cnt[0] + h_cnt[1];
+            cur ^= 1;
+            std::swap(ccur, cnxt);
+        }
+        PADO_LAUNCH("bp_finish_kernel", s,
+                    bp_finish_kernel<<<grid_for((uint64_t)n * K, 256), 256, 0, s>>>(st));
         PADO_CUDA(cudaEventRecord(e1, s));
         PADO_CUDA(cudaEventSynchronize(e1));
         PADO_CUDA(cudaEventElapsedTime(&res.ms, e0, e1));
     } catch (...) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        cudaFreeHost(h_cnt);
+        if (h_cnt) cudaFreeHost(h_cnt);
         throw;
     }
     cudaEventDestroy(e0);

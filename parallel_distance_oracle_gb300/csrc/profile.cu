@@ -66,8 +66,8 @@ void collect_locked()
 
 const char *work_slot_name(int i)
 {
-    static const char *names[WORK_SLOTS] = {"pull_kernel",      "mark_kernel",      "bp_level_kernel",
-                                            "bp_parent_kernel",  "query_unw_kernel", "query_w_kernel",
+    static const char *names[WORK_SLOTS] = {"pull_kernel",      "mark_kernel",      "bp_sibling_kernel",
+                                            "bp_child_kernel",  "query_unw_kernel", "query_w_kernel",
                                             "w_pull_kernel",    "w_mark_kernel",    "finalize_kernel",
                                             "pull.cycles.scan", "pull.cycles.bp",   "pull.cycles.dist",
                                             "pull.cycles.commit", "pull.cycles.heavy"};
