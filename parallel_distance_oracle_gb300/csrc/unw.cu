@@ -330,6 +330,10 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     d.used = d_used.p;
     d.bpd = d_bpd;
     d.bps = d_bps;
+    DBuf<uint8_t> bpmin(std::max<uint32_t>(n, 1));
+    if (K && n)
+        PADO_LAUNCH("bpmin_kernel", s, bpmin_kernel<<<grid_for(n, 256), 256, 0, s>>>(d_bpd, n, K, bpmin.p));
+    d.bpmin = bpmin.p;
     d.pool_hub = pool_hub.p;
     d.pool_dist = pool_dist.p;
     d.pool_cap = cap;

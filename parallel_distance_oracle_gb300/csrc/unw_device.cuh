@@ -25,6 +25,7 @@ struct UnwDev {
     const uint8_t *used;
     const uint8_t *bpd;
     const uint64_t *bps;
+    const uint8_t *bpmin;   // per vertex: least BP distance over the roots (255: none)
     uint32_t *pool_hub;
     uint8_t *pool_dist;
     unsigned long long pool_cap;
@@ -55,11 +56,12 @@ struct GDesc {
     uint32_t s, e;           // current batch's id range [s, e)
     uint32_t iter;           // level computed in the current step
     uint32_t state;          // GS_* below
-    uint32_t fcnt[2];        // vertices that gained labels, by step parity
+    uint32_t tc[3];          // tails marked for stamp x, in tc[x % 3]
     uint32_t roff, nr;       // current batch's roots: broots[roff, roff + nr)
     uint32_t bfirst;         // this graph's entries in the per-batch root counts
-    uint32_t pad;
-    uint64_t dm_off;         // offset of the graph's dist_matrix block
+    uint32_t dmp;            // dist_matrix buffer of the current batch (0/1)
+    uint32_t zqp;            // buffer of the batch whose rows are queued for reset
+    uint64_t dm_off;         // offset of the graph's two dist_matrix blocks ([2][B][n])
 };
 enum : uint32_t { GS_START = 0, GS_LEVEL = 1, GS_DONE = 2 };
 
@@ -70,6 +72,16 @@ __device__ __forceinline__ uint32_t gd_u32(const uint32_t &f) { return __ldcg(&f
 __device__ __forceinline__ uint64_t gd_u64(const uint64_t &f)
 {
     return (uint64_t)__ldcg(reinterpret_cast<const unsigned long long *>(&f));
+}
+
+// bpmin[v] = least BP distance of v over the K roots (255 if none reaches it).
+__global__ void bpmin_kernel(const uint8_t *bpd, uint32_t n, uint32_t K, uint8_t *bpmin)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        uint32_t m = U8_INF;
+        for (uint32_t i = 0; i < K; ++i) m = min(m, (uint32_t)bpd[(uint64_t)v * K + i]);
+        bpmin[v] = (uint8_t)m;
+    }
 }
 
 __device__ __forceinline__ uint32_t warp_min_u32(uint32_t v)
@@ -163,10 +175,10 @@ __device__ void dm_rows_phase(const UnwDev &d, const uint32_t *roots, uint32_t n
         const uint32_t r = roots[q];
         uint8_t *row;
         uint32_t hb = 0;
-        if (gmap) {
+        if (gmap) {  // reset of a finished batch: its buffer is zqp
             const GDesc &x = gd[gmap[r]];
             hb = x.base;
-            row = d.dm + x.dm_off + (uint64_t)((r - hb) % d.B) * x.n;  // fields fixed for the launch
+            row = d.dm + x.dm_off + ((uint64_t)gd_u32(x.zqp) * d.B + (r - hb) % d.B) * x.n;
         } else {
             row = (dm ? dm : d.dm) + (uint64_t)(r - s) * d.n;
         }
@@ -388,7 +400,9 @@ __device__ __forceinline__ BatchCtx tail_ctx(const UnwDev &d, const PullArgs &a,
     if (!a.gmap) return BatchCtx{a.s, a.e_roots, a.b, a.iter, 0u, d.n, a.dm ? a.dm : d.dm, 0u};
     const uint32_t g = a.gmap[t];
     const GDesc &x = a.gd[g];
-    return BatchCtx{gd_u32(x.s), gd_u32(x.e), gd_u32(x.b), gd_u32(x.iter), x.base, x.n, d.dm + x.dm_off, g};
+    return BatchCtx{gd_u32(x.s),    gd_u32(x.e), gd_u32(x.b),
+                    gd_u32(x.iter), x.base,      x.n,
+                    d.dm + x.dm_off + (uint64_t)gd_u32(x.dmp) * d.B * x.n, g};
 }
 
 // Marks the tails of head h for the level stamped `stamp`: neighbours t > mn
@@ -397,7 +411,8 @@ __device__ __forceinline__ BatchCtx tail_ctx(const UnwDev &d, const PullArgs &a,
 // A warp scans 32 entries per step; warp w of `nw` starts at chunk w.
 __device__ __forceinline__ void mark_tails(const UnwDev &d, uint32_t h, uint32_t mn, uint32_t stamp, uint32_t *tails,
                                            uint32_t *tails_cnt, uint32_t *htails, uint32_t *htails_cnt, int lane,
-                                           uint32_t w, uint32_t nw, unsigned long long &bytes)
+                                           uint32_t w, uint32_t nw, unsigned long long &bytes,
+                                           uint32_t *gcnt = nullptr)
 {
     const uint32_t e_end = d.off[h + 1];
     for (uint32_t e0 = d.off[h] + 32 * w; e0 < e_end; e0 += 32 * nw) {
@@ -416,7 +431,9 @@ __device__ __forceinline__ void mark_tails(const UnwDev &d, uint32_t h, uint32_t
                 appended = true;
             }
         }
-        bytes += __popc(__ballot_sync(FULL, appended)) * 8ull;
+        const uint32_t na = __popc(__ballot_sync(FULL, appended));
+        bytes += na * 8ull;
+        if (gcnt && na && lane == 0) atomicAdd(gcnt, na);  // the head's graph's tails for this stamp
         if (__ballot_sync(FULL, in && !ok)) break;
     }
 }
@@ -480,11 +497,13 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
     const uint8_t tr0d = __shfl_sync(FULL, td0, 0);
     const ulonglong2 tr0s = make_ulonglong2(__shfl_sync(FULL, ts0.x, 0), __shfl_sync(FULL, ts0.y, 0));
+    const uint32_t tmin = d.K ? d.bpmin[t] : (uint32_t)U8_INF;
     for (uint32_t c = tid; c < noff; c += blockDim.x) {
         const uint16_t idx = hs.offered[c];
         const uint64_t rr = s + idx;
-        if (d.K == 0 ||
-            !bp_one(d.bpd[rr * d.K], reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K], tr0d, tr0s, iter))
+        if (d.K == 0 || (uint32_t)d.bpmin[rr] + tmin > iter + 2u)  // cannot be covered: no second stage
+            hs.surv[atomicAdd(&hs.ctr[1], 1u)] = idx | 0x8000u;
+        else if (!bp_one(d.bpd[rr * d.K], reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K], tr0d, tr0s, iter))
             hs.surv[atomicAdd(&hs.ctr[1], 1u)] = idx;
     }
     __syncthreads();
@@ -493,14 +512,18 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         if (tid == 0) hs.ctr[1] = 0;
         __syncthreads();
         for (uint32_t c = warp; c < nsurv1; c += blockDim.x >> 5) {
-            const uint16_t idx = hs.surv[c];
-            const bool cov = bp_covered_warp(d, s + idx, lane, 1, td0, ts0, td1, ts1, iter);
+            const uint16_t ent = hs.surv[c];
+            const uint16_t idx = ent & 0x7fffu;
+            const bool cov = !(ent & 0x8000u) && bp_covered_warp(d, s + idx, lane, 1, td0, ts0, td1, ts1, iter);
             if (!cov && lane == 0) hs.offered[atomicAdd(&hs.ctr[1], 1u)] = idx;
         }
         __syncthreads();
         // survivors now sit in `offered`; move them back for the distance test
         const uint32_t ns2 = hs.ctr[1];
         for (uint32_t c = tid; c < ns2; c += blockDim.x) hs.surv[c] = hs.offered[c];
+        __syncthreads();
+    } else {
+        for (uint32_t c = tid; c < nsurv1; c += blockDim.x) hs.surv[c] &= 0x7fffu;
         __syncthreads();
     }
     const uint32_t nsurv = hs.ctr[1];
@@ -599,12 +622,12 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             d.last_min[cp][t] = hs.ctr[4];
             d.act_stamp[cp][t] = a.lid_cur;
             if (!a.next_tails) a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
-            if (a.gd_mut) atomicAdd(&a.gd_mut[bc.g].fcnt[cp], 1u);
             bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0) + (hs.ctr[6] ? 10ull * len : 0);
         }
         if (a.next_tails)
             mark_tails(d, t, hs.ctr[4], a.next_stamp, a.next_tails, a.next_tails_cnt, a.next_htails,
-                       a.next_htails_cnt, lane, warp, blockDim.x >> 5, bytes);
+                       a.next_htails_cnt, lane, warp, blockDim.x >> 5, bytes,
+                       a.gd_mut ? &a.gd_mut[bc.g].tc[a.next_stamp % 3] : nullptr);
     }
     for (uint32_t x = tid; x < d.words; x += blockDim.x) d.ind[(uint64_t)t * d.words + x] = hs.ind[x];
     if (tid == 0) d.ind_stamp[t] = bc.b + 1;
@@ -687,40 +710,64 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
     const uint8_t tr0d = __shfl_sync(FULL, td0, 0);
     const ulonglong2 tr0s = make_ulonglong2(__shfl_sync(FULL, ts0.x, 0), __shfl_sync(FULL, ts0.y, 0));
+    // Any root i gives td_i >= bpmin[r] + bpmin[t], so a pair with
+    // bpmin[r] + bpmin[t] - 2 > iter cannot be covered: it survives BP without
+    // a row load (flag 0x8000: no second stage).
+    const uint32_t tmin = d.K ? d.bpmin[t] : (uint32_t)U8_INF;
     uint32_t nsurv = 0;
     for (uint32_t c0 = 0; c0 < noff; c0 += 32) {
         const uint32_t c = c0 + lane;
         bool keep = false;
-        uint16_t idx = 0;
+        uint16_t ent = 0;
         if (c < noff) {
-            idx = wr.offered[c];
+            const uint16_t idx = wr.offered[c];
             const uint64_t rr = s + idx;
-            keep = d.K == 0 || !bp_one(d.bpd[rr * d.K], reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K], tr0d,
-                                       tr0s, iter);
+            if (d.K == 0 || (uint32_t)d.bpmin[rr] + tmin > iter + 2u) {
+                keep = true;
+                ent = idx | 0x8000u;
+            } else {
+                keep = !bp_one(d.bpd[rr * d.K], reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K], tr0d, tr0s,
+                               iter);
+                ent = idx;
+            }
         }
         const uint32_t km = __ballot_sync(FULL, keep);
         __syncwarp();
-        if (keep) wr.offered[nsurv + __popc(km & ((1u << lane) - 1u))] = idx;
+        if (keep) wr.offered[nsurv + __popc(km & ((1u << lane) - 1u))] = ent;
         nsurv += __popc(km);
         __syncwarp();
     }
     if (d.K > 1 && nsurv) {
+        // second stage for the unflagged survivors, two candidates per step
         uint32_t n2 = 0;
-        for (uint32_t c = 0; c < nsurv; c += 2) {
-            const uint16_t ia = wr.offered[c];
-            const bool two = c + 1 < nsurv;
-            const uint16_t ib = two ? wr.offered[c + 1] : ia;
-            const uint32_t cov = bp_covered_pair(d, s + ia, s + ib, two, lane, 1, td0, ts0, td1, ts1, iter);
-            const bool ca = cov & 1u, cb = two && (cov & 2u);
-            __syncwarp();
-            if (lane == 0) {
-                if (!ca) wr.offered[n2] = ia;
-                if (two && !cb) wr.offered[n2 + (ca ? 0 : 1)] = ib;
+        for (uint32_t c0 = 0; c0 < nsurv; c0 += 32) {
+            const uint32_t c = c0 + lane;
+            const bool in = c < nsurv;
+            const uint16_t ent = in ? wr.offered[c] : (uint16_t)0;
+            uint32_t need = __ballot_sync(FULL, in && !(ent & 0x8000u));
+            bool covered = false;
+            while (need) {
+                const int ka = __ffs(need) - 1;
+                need &= need - 1;
+                const bool two = need != 0;
+                const int kb = two ? __ffs(need) - 1 : ka;
+                if (two) need &= need - 1;
+                const uint32_t ia = __shfl_sync(FULL, (uint32_t)ent, ka), ib = __shfl_sync(FULL, (uint32_t)ent, kb);
+                const uint32_t cov = bp_covered_pair(d, s + ia, s + ib, two, lane, 1, td0, ts0, td1, ts1, iter);
+                if (lane == ka && (cov & 1u)) covered = true;
+                if (two && lane == kb && (cov & 2u)) covered = true;
             }
-            n2 += (ca ? 0 : 1) + (two && !cb ? 1 : 0);
+            const bool keep = in && !covered;
+            const uint32_t km = __ballot_sync(FULL, keep);
+            __syncwarp();
+            if (keep) wr.offered[n2 + __popc(km & ((1u << lane) - 1u))] = ent & 0x7fffu;
+            n2 += __popc(km);
             __syncwarp();
         }
         nsurv = n2;
+    } else {
+        for (uint32_t c = lane; c < nsurv; c += 32) wr.offered[c] &= 0x7fffu;
+        __syncwarp();
     }
     tick(W_CYC_BP);
     // (d) distance test against t's labels with d < iter.  Those labels are
@@ -821,11 +868,10 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             d.last_min[cp][t] = mn;
             d.act_stamp[cp][t] = a.lid_cur;
             if (!a.next_tails) a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
-            if (a.gd_mut) atomicAdd(&a.gd_mut[bc.g].fcnt[cp], 1u);
         }
         if (a.next_tails)
             mark_tails(d, t, mn, a.next_stamp, a.next_tails, a.next_tails_cnt, a.next_htails, a.next_htails_cnt, lane,
-                       0, 1, bytes);
+                       0, 1, bytes, a.gd_mut ? &a.gd_mut[bc.g].tc[a.next_stamp % 3] : nullptr);
     }
     for (uint32_t x = lane; x < d.words; x += 32) d.ind[(uint64_t)t * d.words + x] = wr.ind[x];
     if (lane == 0) d.ind_stamp[t] = bc.b + 1;

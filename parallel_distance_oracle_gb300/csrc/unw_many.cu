@@ -7,15 +7,19 @@
 // [base_g, base_g + n_g) of a disjoint-union CSR -- and ONE persistent
 // cooperative launch advances every graph by one BFS level per step:
 //
-//   step L (stamp L):
-//     A. reset the dist_matrix rows of graphs that finished a batch at step
-//        L-1; self-label the roots of graphs that start a batch (stamp L);
-//        mark the tails of every vertex that gained labels at step L-1.
-//     B. fill the dist_matrix rows of the new batches' roots; pull (the same
-//        warp-per-tail / block-per-heavy-tail code as the one-graph labeler)
-//        with each tail reading its own graph's batch, level and rows.
-//     C. per graph: a graph whose level produced no labels ends its batch and
-//        queues the next batch's roots; the others go one level deeper.
+//   step L (stamp L), one pass then a grid barrier:
+//     A. reset the dist_matrix rows of batches that ended at step L-1; give the
+//        roots of graphs that start a batch their self labels (stamp L), fill
+//        their dist_matrix rows and mark their tails for L+1; pull (the same
+//        warp-per-tail / block-per-heavy-tail code as the one-graph labeler,
+//        each tail reading its own graph's batch, level and rows), every tail
+//        that gains labels marking its tails for L+1 at once.  Each graph has
+//        two dist_matrix buffers used by alternate batches, so the reset of
+//        the old batch and the fill of the new one never share a row.
+//     C. (after the barrier) a warp per graph: a graph with no tails for L+1
+//        ends its batch -- its next level would add nothing -- and queues the
+//        next batch's roots; the others go one level deeper.  A second barrier
+//        publishes the new per-graph state.
 //
 // Each graph runs exactly the reference's batch sequence (batches of B
 // consecutive ranks of that graph, pado_unw_unv_unp.h:1080-1118) and, within
@@ -39,16 +43,16 @@
 namespace pado {
 namespace {
 
-enum ManyPhase : uint32_t { MP_STEP = 0, MP_A_RETRY = 1, MP_B_RETRY = 2, MP_DONE = 3 };
+enum ManyPhase : uint32_t { MP_STEP = 0, MP_RETRY = 1, MP_DONE = 2 };
 enum ManyExit : uint32_t { MX_RUNNING = 0, MX_DONE = 1, MX_NEED_POOL = 2, MX_OVERFLOW = 3 };
 
 struct ManyCtl {
     GridBar bar;
     uint32_t phase, lid, active, steps;
-    uint32_t front_cnt[2], tails_cnt[2], htails_cnt[2];
-    uint32_t rq_cnt[2];   // roots to self-label in step L: rq[L & 1]
-    uint32_t zq_cnt[2];   // roots whose dist_matrix rows are reset in step L
-    uint32_t rr_cnt, retry_cnt, status, exit_code;
+    uint32_t tcnt[3], hcnt[3];  // light / heavy tails marked for stamp x, in slot x % 3
+    uint32_t rq_cnt[2];         // roots to start in step L: rq[L & 1]
+    uint32_t zq_cnt[2];         // roots whose dist_matrix rows are reset in step L
+    uint32_t rr_cnt, rretry_cnt, tretry_cnt, status, exit_code, pad;
 };
 
 struct ManyBufs {
@@ -58,37 +62,81 @@ struct ManyBufs {
     const uint32_t *bcnt;      // roots per batch (graph g's batch b at gd[g].bfirst + b)
     uint32_t G;
     uint32_t *rq[2], *zq[2], *rr;
-    uint32_t *front[2];
-    uint32_t *tails, *htails, *retry;
+    uint32_t *tails[3], *htails[3];
+    uint32_t *rretry, *tretry;
 };
+
+// Batch start for roots[0, nr) of graphs in GS_START: self label at stamp L,
+// the dist_matrix row of the root in its graph's current buffer, tails for L+1.
+__device__ void many_root_step(const UnwDev &d, const ManyBufs &bf, ManyCtl *c, const uint32_t *roots, uint32_t nr,
+                               uint32_t L)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const int p = L & 1, nx = (L + 1) % 3;
+    unsigned long long bytes = 0;
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nr; q += nw) {
+        const uint32_t r = roots[q];
+        const uint32_t g = bf.gmap[r];
+        const GDesc &x = bf.gd[g];
+        const uint32_t gs = gd_u32(x.s), gb = gd_u32(x.b), gbase = x.base, gn = x.n;
+        uint8_t *dm = d.dm + x.dm_off + (uint64_t)gd_u32(x.dmp) * d.B * gn;
+        uint64_t base;
+        if (!warp_reserve(d, r, d.lab_len[r] + 1, base, lane)) {
+            if (lane == 0) {
+                atomicOr(d.status, ST_POOL_RETRY);
+                bf.rretry[atomicAdd(&c->rretry_cnt, 1u)] = r;
+            }
+            continue;
+        }
+        const uint32_t len = d.lab_len[r];
+        const uint32_t idx = r - gs;
+        for (uint32_t w = lane; w < d.words; w += 32)
+            d.ind[(uint64_t)r * d.words + w] = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
+        if (lane == 0) {
+            d.pool_hub[base + len] = r;
+            d.pool_dist[base + len] = 0;
+            d.lab_len[r] = len + 1;
+            d.last_pos[p][r] = base + len;
+            d.last_cnt[p][r] = 1;
+            d.last_min[p][r] = r;
+            d.act_stamp[p][r] = L;
+            d.ind_stamp[r] = gb + 1;
+        }
+        __syncwarp();
+        uint8_t *row = dm + (uint64_t)idx * gn;
+        for (uint32_t j = lane; j <= len; j += 32) row[d.pool_hub[base + j] - gbase] = d.pool_dist[base + j];
+        mark_tails(d, r, r, L + 1, bf.tails[nx], &c->tcnt[nx], bf.htails[nx], &c->hcnt[nx], lane, 0, 1, bytes,
+                   &bf.gd[g].tc[nx]);
+    }
+    if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_MARK], bytes);
+}
 
 // Step bookkeeping, a warp per graph (see the file comment, part C).
 __device__ void many_bookkeep(const UnwDev &d, ManyCtl *c, const ManyBufs &bf, uint32_t L)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const int cp = L & 1, np = (L + 1) & 1;
+    const int nx = (L + 1) % 3, nn = (L + 2) % 3, np = (L + 1) & 1;
     for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < bf.G; g += nw) {
         GDesc &x = bf.gd[g];
         // every lane reads the descriptor before lane 0 rewrites it
         const uint32_t st = vload(&x.state);
         if (st == GS_DONE) continue;
-        const uint32_t fc = vload(&x.fcnt[cp]);
+        const uint32_t nt = vload(&x.tc[nx]);
         const uint32_t xb = vload(&x.b), xnr = vload(&x.nr), xroff = vload(&x.roff), xiter = vload(&x.iter);
+        const uint32_t xdmp = vload(&x.dmp);
         const uint32_t xnb = x.nb, xbf = x.bfirst, xbase = x.base, xn = x.n;
         __syncwarp();
-        if (st == GS_START) {
+        if (nt != 0) {
             if (lane == 0) {
+                const uint32_t it = st == GS_START ? 1u : xiter + 1;
+                if (it >= U8_INF) atomicOr(&c->status, ST_LEVEL_OVERFLOW);
+                x.iter = it;
                 x.state = GS_LEVEL;
-                x.iter = 1;
-            }
-        } else if (fc != 0) {
-            if (lane == 0) {
-                if (xiter + 1 >= U8_INF) atomicOr(&c->status, ST_LEVEL_OVERFLOW);
-                x.iter = xiter + 1;
             }
         } else {
-            // batch done: its rows are reset at the next step
+            // batch over: its rows are reset at the next step
             uint32_t pos = 0;
             if (lane == 0) pos = atomicAdd(&c->zq_cnt[np], xnr);
             pos = __shfl_sync(FULL, pos, 0);
@@ -102,6 +150,8 @@ __device__ void many_bookkeep(const UnwDev &d, ManyCtl *c, const ManyBufs &bf, u
                 pos = __shfl_sync(FULL, pos, 0);
                 for (uint32_t j = lane; j < nr; j += 32) bf.rq[np][pos + j] = bf.broots[roff + j];
                 if (lane == 0) {
+                    x.zqp = xdmp;
+                    x.dmp = xdmp ^ 1u;
                     x.b = b;
                     x.s = xbase + b * d.B;
                     x.e = min(x.s + d.B, xbase + xn);
@@ -111,11 +161,12 @@ __device__ void many_bookkeep(const UnwDev &d, ManyCtl *c, const ManyBufs &bf, u
                     x.state = GS_START;
                 }
             } else if (lane == 0) {
+                x.zqp = xdmp;
                 x.state = GS_DONE;
                 atomicSub(&c->active, 1u);
             }
         }
-        if (lane == 0) x.fcnt[np] = 0;  // counted during step L+1
+        if (lane == 0) x.tc[nn] = 0;  // counted during step L+1
         __syncwarp();
     }
 }
@@ -135,47 +186,37 @@ __global__ void __launch_bounds__(PULL_THREADS, 4) many_loop_kernel(UnwDev d, Ma
             return;
         }
         const uint32_t L = vload(&c->lid) + 1;
-        const int cp = L & 1, pp = (L - 1) & 1;
-        PullArgs a{bf.tails, &c->tails_cnt[cp], bf.htails, &c->htails_cnt[cp], 0u, 0u, 0u, 0u, L,
-                   bf.front[cp], &c->front_cnt[cp], bf.retry, &c->retry_cnt, bf.gd, bf.gmap, bf.gd};
-        if (phase == MP_STEP || phase == MP_A_RETRY) {
-            if (phase == MP_STEP) {
-                dm_rows_phase(d, bf.zq[cp], vload(&c->zq_cnt[cp]), 0u, 0, bf.gd, bf.gmap);
-                root_init_phase(d, bf.rq[cp], vload(&c->rq_cnt[cp]), 0u, 0u, L, bf.front[cp], &c->front_cnt[cp],
-                                bf.retry, &c->retry_cnt, bf.gd, bf.gmap);
-                mark_phase(d, bf.front[pp], vload(&c->front_cnt[pp]), L, bf.tails, &c->tails_cnt[cp], bf.htails,
-                           &c->htails_cnt[cp]);
-            } else {
-                root_init_phase(d, bf.rr, vload(&c->rr_cnt), 0u, 0u, L, bf.front[cp], &c->front_cnt[cp], bf.retry,
-                                &c->retry_cnt, bf.gd, bf.gmap);
-            }
-            if (!grid_barrier(&c->bar, &c->status)) return;
-            if (vload(&c->retry_cnt)) {
-                if (leader) {
-                    c->phase = MP_A_RETRY;
-                    c->exit_code = MX_NEED_POOL;
-                }
-                return;
-            }
-            dm_rows_phase(d, bf.rq[cp], vload(&c->rq_cnt[cp]), 0u, 1, bf.gd, bf.gmap);
+        const int cur = L % 3, nx = (L + 1) % 3, cp = L & 1;
+        PullArgs a{bf.tails[cur], &c->tcnt[cur], bf.htails[cur], &c->hcnt[cur], 0u, 0u, 0u, 0u, L,
+                   nullptr, nullptr, bf.tretry, &c->tretry_cnt, bf.gd, bf.gmap, bf.gd};
+        a.next_tails = bf.tails[nx];
+        a.next_tails_cnt = &c->tcnt[nx];
+        a.next_htails = bf.htails[nx];
+        a.next_htails_cnt = &c->hcnt[nx];
+        a.next_stamp = L + 1;
+        if (phase == MP_STEP) {
+            dm_rows_phase(d, bf.zq[cp], vload(&c->zq_cnt[cp]), 0u, 0, bf.gd, bf.gmap);
+            many_root_step(d, bf, c, bf.rq[cp], vload(&c->rq_cnt[cp]), L);
+        } else {
+            many_root_step(d, bf, c, bf.rr, vload(&c->rr_cnt), L);
         }
         pull_phase(d, a, pull_smem);
+        if (leader) {
+            c->tcnt[(L + 2) % 3] = 0;
+            c->hcnt[(L + 2) % 3] = 0;
+        }
         if (!grid_barrier(&c->bar, &c->status)) return;
-        if (vload(&c->retry_cnt)) {
+        if (vload(&c->rretry_cnt) || vload(&c->tretry_cnt)) {
             if (leader) {
-                c->phase = MP_B_RETRY;
+                c->phase = MP_RETRY;
                 c->exit_code = MX_NEED_POOL;
             }
             return;
         }
         many_bookkeep(d, c, bf, L);
         if (leader) {
-            const int np = (L + 1) & 1;
             c->lid = L;
             c->steps += 1;
-            c->front_cnt[np] = 0;
-            c->tails_cnt[np] = 0;
-            c->htails_cnt[np] = 0;
             c->rq_cnt[cp] = 0;
             c->zq_cnt[cp] = 0;
             c->phase = MP_STEP;
@@ -228,7 +269,7 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
         x.n = ng;
         x.nb = (uint32_t)(((uint64_t)ng + B - 1) / B);
         x.bfirst = (uint32_t)bcnt.size();
-        x.dm_off = (uint64_t)B * base;
+        x.dm_off = 2ull * B * base;
         x.state = GS_DONE;
         const uint32_t first_root = (uint32_t)broots.size();
         for (uint32_t v = base; v < base + ng; ++v) hgmap[v] = (uint16_t)gi;
@@ -268,8 +309,8 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
     DBuf<uint32_t> lab_len(n), lab_cap(n), last_cnt0(n), last_cnt1(n), last_min0(n), last_min1(n);
     DBuf<uint32_t> act_stamp0(n), act_stamp1(n), tail_stamp(n), ind_stamp(n);
     DBuf<uint32_t> ind((uint64_t)n * words);
-    DBuf<uint8_t> dm((uint64_t)B * n);
-    DBuf<uint32_t> front0(n), front1(n), tails(n), htails(n), retry(n), status(1);
+    DBuf<uint8_t> dm(2ull * B * n);  // two buffers per graph, by batch
+    DBuf<uint32_t> tl0(n), tl1(n), tl2(n), th0(n), th1(n), th2(n), rretry(n), tretry(n), status(1);
     DBuf<uint32_t> rq0b(n), rq1b(n), zq0b(n), zq1b(n), rr(n);
     DBuf<GDesc> d_gd(G);
     DBuf<uint16_t> d_gmap(std::max<uint32_t>(n, 1));
@@ -309,6 +350,10 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
     d.used = d_used.p;
     d.bpd = d_bpd;
     d.bps = d_bps;
+    DBuf<uint8_t> bpmin(std::max<uint32_t>(n, 1));
+    if (K && n)
+        PADO_LAUNCH("bpmin_kernel", s, bpmin_kernel<<<grid_for(n, 256), 256, 0, s>>>(d_bpd, n, K, bpmin.p));
+    d.bpmin = bpmin.p;
     d.pool_hub = pool_hub.p;
     d.pool_dist = pool_dist.p;
     d.pool_cap = cap;
@@ -331,8 +376,8 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
     d.status = status.p;
     d.work = work_counters();
 
-    ManyBufs bf{d_gd.p, d_gmap.p, d_broots.p, d_bcnt.p, G, {rq0b.p, rq1b.p}, {zq0b.p, zq1b.p}, rr.p,
-                {front0.p, front1.p}, tails.p, htails.p, retry.p};
+    ManyBufs bf{d_gd.p,           d_gmap.p,           d_broots.p, d_bcnt.p, G, {rq0b.p, rq1b.p}, {zq0b.p, zq1b.p},
+                rr.p,             {tl0.p, tl1.p, tl2.p}, {th0.p, th1.p, th2.p}, rretry.p, tretry.p};
 
     // Grow the pool to hold at least `need` entries (plus slack), keeping content.
     auto grow_pool = [&](unsigned long long need) {
@@ -383,16 +428,17 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
                 unsigned long long top = 0;
                 PADO_CUDA(cudaMemcpy(&top, pool_top.p, 8, cudaMemcpyDeviceToHost));
                 grow_pool(top);
-                if (h.phase == MP_A_RETRY) {
-                    PADO_CUDA(cudaMemcpyAsync(rr.p, retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
-                    h.rr_cnt = h.retry_cnt;
-                } else {
-                    const int cpar = (h.lid + 1) & 1;
-                    PADO_CUDA(cudaMemcpyAsync(tails.p, retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
-                    h.tails_cnt[cpar] = h.retry_cnt;
-                    h.htails_cnt[cpar] = 0;
-                }
-                h.retry_cnt = 0;
+                // failed roots run again from rr; failed tails become the whole light
+                // list of the step (any degree is fine there)
+                PADO_CUDA(cudaMemcpyAsync(rr.p, rretry.p, h.rretry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
+                h.rr_cnt = h.rretry_cnt;
+                const int cur = (h.lid + 1) % 3;
+                uint32_t *lists[3] = {tl0.p, tl1.p, tl2.p};
+                PADO_CUDA(cudaMemcpyAsync(lists[cur], tretry.p, h.tretry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
+                h.tcnt[cur] = h.tretry_cnt;
+                h.hcnt[cur] = 0;
+                h.rretry_cnt = 0;
+                h.tretry_cnt = 0;
                 h.status = 0;
                 h.exit_code = MX_RUNNING;
                 PADO_CUDA(cudaMemcpyAsync(ctl.p, &h, sizeof(ManyCtl), cudaMemcpyHostToDevice, s));
