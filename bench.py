@@ -300,6 +300,7 @@ def main():
         for i in range(args.steps):
             t0 = time.perf_counter()
             idx = build_once()
+            tb = time.perf_counter()
             d2h = export(idx)
             t1 = time.perf_counter()
             info = idx.info()
@@ -307,7 +308,7 @@ def main():
             dev_s.append(info.build_seconds)
             wall_s.append(t1 - t0)
             log(f"step {i}: labels={labels} device={info.build_seconds:.4f}s (bp {info.bp_seconds:.4f}s) "
-                f"wall={t1 - t0:.3f}s levels={info.levels}")
+                f"wall={t1 - t0:.3f}s (build {tb - t0:.3f}s, export {t1 - tb:.3f}s) levels={info.levels}")
             if i < args.steps - 1:
                 idx.close()
     barrier()

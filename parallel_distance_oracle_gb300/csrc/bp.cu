@@ -318,7 +318,7 @@ void bp_select(const HostGraph &hg, uint32_t lo, uint32_t hi, uint32_t K, std::v
         seeds[i].push_back({r, 0, 0});
         int ns = 0;
         for (uint32_t k = hg.off[r + 1]; k > hg.off[r]; --k) {
-            const uint32_t v = hg.adj[k - 1];
+            const uint32_t v = hg.adjp()[k - 1];
             if (!used[v]) {
                 used[v] = 1;
                 seeds[i].push_back({v, 1, 1ULL << ns});

@@ -2,6 +2,8 @@
 // relabeling, export/import, queries and the reference's index file format.
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -98,7 +100,15 @@ void check_graph(uint32_t n, const uint64_t *off, const uint32_t *adj)
     for (uint32_t v = 0; v < n; ++v) PADO_CHECK(off[v + 1] >= off[v], PADO_E_ARG, "offsets must be non-decreasing");
     PADO_CHECK(off[n] < (1ull << 32), PADO_E_ARG, "more than 2^32-1 adjacency entries");
     PADO_CHECK(off[n] == 0 || adj != nullptr, PADO_E_ARG, "null adjacency");
-    for (uint64_t e = 0; e < off[n]; ++e) PADO_CHECK(adj[e] < n, PADO_E_ARG, "adjacency id out of range");
+    std::atomic<bool> bad{false};
+    parallel_ranges(n, [&](uint32_t lo, uint32_t hi) {
+        for (uint64_t e = off[lo]; e < off[hi]; ++e)
+            if (adj[e] >= n) {
+                bad = true;
+                return;
+            }
+    });
+    PADO_CHECK(!bad, PADO_E_ARG, "adjacency id out of range");
 }
 
 void check_rank(uint32_t n, const uint32_t *rank)
@@ -114,14 +124,14 @@ void check_rank(uint32_t n, const uint32_t *rank)
 void upload_graph(const pado::HostGraph &hg, pado::DevGraph &g, bool weighted, cudaStream_t s)
 {
     g.n = hg.n;
-    g.m = hg.adj.size();
+    g.m = hg.m();
     g.off.alloc(hg.n + 1);
     g.off.upload(hg.off.data(), hg.n + 1, s);
     g.adj.alloc(std::max<uint64_t>(g.m, 1));
-    g.adj.upload(hg.adj.data(), g.m, s);
+    g.adj.upload(hg.adjp(), g.m, s);
     if (weighted) {
         g.w.alloc(std::max<uint64_t>(g.m, 1));
-        g.w.upload(hg.w.data(), g.m, s);
+        g.w.upload(hg.wp(), g.m, s);
     }
 }
 
@@ -131,10 +141,20 @@ int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t 
     if (!out) return fail(PADO_E_ARG, "null output handle");
     *out = nullptr;
     return guarded([&] {
+        // PADO_TRACE=1: host phases of the build on stderr
+        const bool trace = std::getenv("PADO_TRACE") != nullptr;
+        auto t_prev = std::chrono::steady_clock::now();
+        auto phase = [&](const char *what) {
+            if (!trace) return;
+            const auto t = std::chrono::steady_clock::now();
+            fprintf(stderr, "build %s %.3f ms\n", what, std::chrono::duration<double, std::milli>(t - t_prev).count());
+            t_prev = t;
+        };
         PADO_CHECK(B >= 1 && B <= pado::MAX_BATCH, PADO_E_ARG, "batch size must be in [1, 2048]");
         PADO_CHECK(K <= pado::MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
         PADO_CHECK(!weighted || w != nullptr || (off && off[n] == 0), PADO_E_ARG, "null weights");
         check_graph(n, off, adj);
+        phase("check");
         if (rank) check_rank(n, rank);
         std::unique_ptr<pado_index> h(new pado_index);
         PADO_CUDA(cudaGetDevice(&h->device));
@@ -146,19 +166,24 @@ int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t 
         PADO_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
         struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
         pado::HostGraph hg = pado::relabel_host(n, off, adj, weighted ? w : nullptr, rank);
+        phase("relabel");
         pado::DevGraph g;
         upload_graph(hg, g, weighted, s);
         if (rank) {
             h->rank.alloc(std::max<uint32_t>(n, 1));
             h->rank.upload(rank, n, s);
         }
+        if (trace) PADO_CUDA(cudaStreamSynchronize(s));
+        phase("upload");
         pado::LabelRun run;
         if (!weighted) {
             std::vector<uint8_t> used(n, 0);
             h->bpd.alloc(std::max<uint64_t>((uint64_t)n * K, 1));
             h->bps.alloc(std::max<uint64_t>((uint64_t)n * K * 2, 1));
             pado::BpResult bp = pado::bp_label(hg, g, K, used, h->bpd.p, h->bps.p, s);
+            phase("bit-parallel");
             run = pado::unw_label(g, K, B, used, h->bpd.p, h->bps.p, h->store, s);
+            phase("labeling");
             h->info.bp_seconds = bp.ms * 1e-3;
             h->info.build_seconds = (bp.ms + run.ms) * 1e-3;
             h->info.levels = run.levels + bp.levels;
@@ -177,6 +202,27 @@ int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t 
         h->info.device_bytes = h->device_bytes();
         *out = h.release();
     });
+}
+
+// Export in original-id order: vertex v takes the list (and BP row) of rank[v].
+__global__ void __launch_bounds__(256) export_permute_kernel(uint32_t n, uint32_t K, int bp, const uint32_t *rank,
+                                                             const uint64_t *roff, const uint64_t *noff,
+                                                             const uint32_t *hub, const uint8_t *dist, uint32_t dsz,
+                                                             const uint8_t *bpd, const uint64_t *bps, uint32_t *ohub,
+                                                             uint8_t *odist, uint8_t *obpd, uint64_t *obps)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nw) {
+        const uint32_t r = rank[v];
+        const uint64_t b = roff[r], len = roff[r + 1] - b, o = noff[v];
+        for (uint64_t j = lane; j < len; j += 32) ohub[o + j] = hub[b + j];
+        for (uint64_t j = lane; j < len * dsz; j += 32) odist[o * dsz + j] = dist[b * dsz + j];
+        if (bp) {
+            for (uint32_t i = lane; i < K; i += 32) obpd[(uint64_t)v * K + i] = bpd[(uint64_t)r * K + i];
+            for (uint32_t i = lane; i < 2 * K; i += 32) obps[(uint64_t)v * K * 2 + i] = bps[(uint64_t)r * K * 2 + i];
+        }
+    }
 }
 
 // Many graphs laid side by side: graph i relabeled by its rank and shifted to
@@ -221,7 +267,8 @@ UnionGraph union_graph(uint32_t G, const uint32_t *n, const uint64_t *const *off
                     if (rank && rank[gi]) check_rank(ng, rank[gi]);
                     pado::HostGraph one = pado::relabel_host(ng, off[gi], adj[gi], nullptr, rank ? rank[gi] : nullptr);
                     for (uint32_t v = 0; v < ng; ++v) hg.off[base + v + 1] = abase[i] + one.off[v + 1];
-                    for (size_t k = 0; k < one.adj.size(); ++k) hg.adj[abase[i] + k] = one.adj[k] + base;
+                    const uint32_t *oa = one.adjp();
+                    for (uint64_t k = 0; k < one.m(); ++k) hg.adj[abase[i] + k] = oa[k] + base;
                 }
             } catch (const std::exception &e) {
                 errs[t] = e.what();
@@ -332,6 +379,25 @@ HostGraph relabel_host(uint32_t n, const uint64_t *off, const uint32_t *adj, con
     g.n = n;
     g.off.assign(n + 1, 0);
     const uint64_t m = off[n];
+    if (!rank) {
+        // already ranked: used in place when every list is in descending
+        // (id, weight) order
+        std::atomic<bool> sorted{true};
+        parallel_ranges(n, [&](uint32_t lo, uint32_t hi) {
+            for (uint32_t v = lo; v < hi && sorted; ++v)
+                for (uint64_t k = off[v] + 1; k < off[v + 1]; ++k)
+                    if (adj[k - 1] < adj[k] || (adj[k - 1] == adj[k] && w && w[k - 1] < w[k])) {
+                        sorted = false;
+                        break;
+                    }
+        });
+        if (sorted) {
+            for (uint32_t v = 0; v <= n; ++v) g.off[v] = (uint32_t)off[v];
+            g.adj_view = adj;
+            g.w_view = w;
+            return g;
+        }
+    }
     g.adj.resize(m);
     if (w) g.w.resize(m);
     if (rank) {
@@ -574,42 +640,47 @@ int pado_export(const pado_index *h, uint64_t *off, uint32_t *hub, void *dist, u
     return guarded([&] {
         PADO_CUDA(cudaSetDevice(h->device));
         const uint32_t n = h->n, K = h->K;
+        const uint64_t tot = h->store.total;
         const size_t dsz = h->kind == PADO_WEIGHTED ? 2 : 1;
+        const void *ddist = dsz == 1 ? (const void *)h->store.dist8.p : (const void *)h->store.dist16.p;
+        const bool bp = K && (bp_dist || bp_sets);
+        cudaStream_t s = cudaStreamPerThread;
+        if (!h->rank.n) {
+            // ids are ranks: the store is already in export order
+            h->store.off.download(off, n + 1, s);
+            h->store.hub.download(hub, tot, s);
+            if (tot) PADO_CUDA(cudaMemcpyAsync(dist, ddist, tot * dsz, cudaMemcpyDeviceToHost, s));
+            if (K && bp_dist) h->bpd.download(bp_dist, (uint64_t)n * K, s);
+            if (K && bp_sets) h->bps.download(bp_sets, (uint64_t)n * K * 2, s);
+            PADO_CUDA(cudaStreamSynchronize(s));
+            return;
+        }
+        // original-id order: offsets on the host, lists and BP rows gathered on
+        // the device, then one copy of each array
         std::vector<uint64_t> roff(n + 1);
-        std::vector<uint32_t> rhub(h->store.total);
-        std::vector<uint8_t> rdist(h->store.total * dsz);
-        h->store.off.download(roff.data(), n + 1);
-        h->store.hub.download(rhub.data(), h->store.total);
-        if (dsz == 1)
-            h->store.dist8.download(rdist.data(), h->store.total);
-        else
-            h->store.dist16.download(reinterpret_cast<int16_t *>(rdist.data()), h->store.total);
-        std::vector<uint32_t> rk;
-        if (h->rank.n) {
-            rk.resize(n);
-            h->rank.download(rk.data(), n);
-        }
-        std::vector<uint8_t> rbpd;
-        std::vector<uint64_t> rbps;
-        if (K && (bp_dist || bp_sets)) {
-            rbpd.resize((size_t)n * K);
-            rbps.resize((size_t)n * K * 2);
-            h->bpd.download(rbpd.data(), rbpd.size());
-            h->bps.download(rbps.data(), rbps.size());
-        }
-        PADO_CUDA(cudaDeviceSynchronize());
+        std::vector<uint32_t> rk(n);
+        h->store.off.download(roff.data(), n + 1, s);
+        h->rank.download(rk.data(), n, s);
+        PADO_CUDA(cudaStreamSynchronize(s));
         off[0] = 0;
-        for (uint32_t v = 0; v < n; ++v) {
-            const uint32_t r = rk.empty() ? v : rk[v];
-            const uint64_t b = roff[r], len = roff[r + 1] - b;
-            off[v + 1] = off[v] + len;
-            if (len) {
-                memcpy(hub + off[v], rhub.data() + b, len * 4);
-                memcpy(static_cast<uint8_t *>(dist) + off[v] * dsz, rdist.data() + b * dsz, len * dsz);
-            }
-            if (K && bp_dist) memcpy(bp_dist + (size_t)v * K, rbpd.data() + (size_t)r * K, K);
-            if (K && bp_sets) memcpy(bp_sets + (size_t)v * K * 2, rbps.data() + (size_t)r * K * 2, K * 16);
-        }
+        for (uint32_t v = 0; v < n; ++v) off[v + 1] = off[v] + (roff[rk[v] + 1] - roff[rk[v]]);
+        pado::DBuf<uint64_t> noff(n + 1);
+        pado::DBuf<uint32_t> thub(std::max<uint64_t>(tot, 1));
+        pado::DBuf<uint8_t> tdist(std::max<uint64_t>(tot * dsz, 1));
+        pado::DBuf<uint8_t> tbpd(bp ? (uint64_t)n * K : 1);
+        pado::DBuf<uint64_t> tbps(bp ? (uint64_t)n * K * 2 : 1);
+        noff.upload(off, n + 1, s);
+        if (n)
+            PADO_LAUNCH("export_permute_kernel", s,
+                        export_permute_kernel<<<pado::grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(
+                            n, K, bp ? 1 : 0, h->rank.p, h->store.off.p, noff.p, h->store.hub.p,
+                            static_cast<const uint8_t *>(ddist), (uint32_t)dsz, h->bpd.p, h->bps.p, thub.p, tdist.p,
+                            tbpd.p, tbps.p));
+        thub.download(hub, tot, s);
+        tdist.download(static_cast<uint8_t *>(dist), tot * dsz, s);
+        if (K && bp_dist) tbpd.download(bp_dist, (uint64_t)n * K, s);
+        if (K && bp_sets) tbps.download(bp_sets, (uint64_t)n * K * 2, s);
+        PADO_CUDA(cudaStreamSynchronize(s));
     });
 }
 

@@ -42,6 +42,14 @@ struct HostGraph {
     std::vector<uint32_t> off;
     std::vector<uint32_t> adj;
     std::vector<uint8_t> w;
+    // When the caller's arrays are already in this form (ids are ranks, lists
+    // descending) they are used in place: the views point at them and adj / w
+    // stay empty.  Such a graph lives no longer than the call that made it.
+    const uint32_t *adj_view = nullptr;
+    const uint8_t *w_view = nullptr;
+    const uint32_t *adjp() const { return adj_view ? adj_view : adj.data(); }
+    const uint8_t *wp() const { return w_view ? w_view : w.data(); }
+    uint64_t m() const { return off.empty() ? 0 : off.back(); }
 };
 HostGraph relabel_host(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w,
                        const uint32_t *rank);
