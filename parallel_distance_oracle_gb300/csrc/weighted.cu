@@ -40,10 +40,20 @@
 // (root, distance) pairs of each vertex are read from a parity-double-
 // buffered log, so heads can be read while their owners accept new roots.
 // dists_table entries carry a batch stamp and never need resetting.
+//
+// Schedule: one persistent cooperative launch (w_loop_kernel) runs every
+// batch -- start (root tables), rounds (mark, then pull), end (filter and
+// buffer reset, then commit) -- with a bounded grid barrier between phases
+// instead of a kernel launch and a host round trip each.  It returns to the
+// host only to grow the round logs or the label pool (the failed tails or
+// vertices are re-run exactly afterwards) or on an error.  PADO_LEVEL_LOOP=host
+// selects the host-driven loop of separate kernels instead.
 
 #include <algorithm>
 #include <climits>
+#include <cstring>
 
+#include "grid_barrier.cuh"
 #include "pado_internal.cuh"
 
 namespace pado {
@@ -126,9 +136,8 @@ __device__ __forceinline__ bool warp_reserve_w(const WDev &d, uint32_t v, uint32
 }
 
 // initialize_tables (pado_weighted_unv_unp.h:281-330)
-__global__ void __launch_bounds__(256) w_root_init_kernel(WDev d, uint32_t s, uint32_t nroots, uint32_t lid0,
-                                                          uint32_t *front, uint32_t *front_cnt, uint32_t *news,
-                                                          uint32_t *news_cnt)
+__device__ void w_root_init_phase(const WDev &d, uint32_t s, uint32_t nroots, uint32_t lid0, uint32_t *front,
+                                  uint32_t *front_cnt, uint32_t *news, uint32_t *news_cnt)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -157,11 +166,17 @@ __global__ void __launch_bounds__(256) w_root_init_kernel(WDev d, uint32_t s, ui
     }
 }
 
-__global__ void __launch_bounds__(256) w_mark_kernel(WDev d, const uint32_t *front, const uint32_t *front_cnt,
-                                                     uint32_t lid_cur, uint32_t *tails, uint32_t *tails_cnt)
+__global__ void __launch_bounds__(256) w_root_init_kernel(WDev d, uint32_t s, uint32_t nroots, uint32_t lid0,
+                                                          uint32_t *front, uint32_t *front_cnt, uint32_t *news,
+                                                          uint32_t *news_cnt)
+{
+    w_root_init_phase(d, s, nroots, lid0, front, front_cnt, news, news_cnt);
+}
+
+__device__ void w_mark_phase(const WDev &d, const uint32_t *front, uint32_t cnt, uint32_t lid_cur, uint32_t *tails,
+                             uint32_t *tails_cnt)
 {
     const int lane = threadIdx.x & 31;
-    const uint32_t cnt = *front_cnt;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const int pp = (lid_cur - 1) & 1;
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw) {
@@ -181,21 +196,27 @@ __global__ void __launch_bounds__(256) w_mark_kernel(WDev d, const uint32_t *fro
     }
 }
 
-__global__ void w_snap_kernel(WDev d, uint32_t rows)
+__global__ void __launch_bounds__(256) w_mark_kernel(WDev d, const uint32_t *front, const uint32_t *front_cnt,
+                                                     uint32_t lid_cur, uint32_t *tails, uint32_t *tails_cnt)
+{
+    w_mark_phase(d, front, *front_cnt, lid_cur, tails, tails_cnt);
+}
+
+__device__ void w_snap_phase(const WDev &d, uint32_t rows)
 {
     const uint64_t tot = (uint64_t)rows * d.B;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tot; i += (uint64_t)gridDim.x * blockDim.x)
         d.snap[i] = d.vd[i];
 }
 
+__global__ void w_snap_kernel(WDev d, uint32_t rows) { w_snap_phase(d, rows); }
+
 // Per-warp dynamic shared memory: rmin[B] int32, res[B] int32, touched[B] u16.
-__global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_pull_kernel(WDev d, const uint32_t *tails, const uint32_t *tails_cnt,
-                                                                  uint32_t s, uint32_t b, uint32_t lid_cur,
-                                                                  uint32_t *front_next, uint32_t *front_next_cnt,
-                                                                  uint32_t *news, uint32_t *news_cnt, uint32_t *retry,
-                                                                  uint32_t *retry_cnt)
+// Run by blocks of WPULL_WARPS warps.
+__device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt, uint32_t s, uint32_t b,
+                             uint32_t lid_cur, uint32_t *front_next, uint32_t *front_next_cnt, uint32_t *news,
+                             uint32_t *news_cnt, uint32_t *retry, uint32_t *retry_cnt, unsigned char *wsm)
 {
-    extern __shared__ __align__(16) unsigned char wsm[];
     __shared__ uint32_t s_cnt[WPULL_WARPS][2];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
@@ -204,7 +225,6 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_pull_kernel(WDev d, con
     int32_t *res = reinterpret_cast<int32_t *>(wsm) + (size_t)WPULL_WARPS * B + (size_t)w * B;
     uint16_t *touched = reinterpret_cast<uint16_t *>(reinterpret_cast<int32_t *>(wsm) + (size_t)2 * WPULL_WARPS * B) +
                         (size_t)w * B;
-    const uint32_t cnt = *tails_cnt;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const int pp = (lid_cur - 1) & 1, cp = lid_cur & 1;
     const uint32_t lid_prev = lid_cur - 1;
@@ -370,9 +390,20 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_pull_kernel(WDev d, con
     if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_WPULL], bytes);
 }
 
+__global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_pull_kernel(WDev d, const uint32_t *tails, const uint32_t *tails_cnt,
+                                                                  uint32_t s, uint32_t b, uint32_t lid_cur,
+                                                                  uint32_t *front_next, uint32_t *front_next_cnt,
+                                                                  uint32_t *news, uint32_t *news_cnt, uint32_t *retry,
+                                                                  uint32_t *retry_cnt)
+{
+    extern __shared__ __align__(16) unsigned char wsm[];
+    w_pull_phase(d, tails, *tails_cnt, s, b, lid_cur, front_next, front_next_cnt, news, news_cnt, retry, retry_cnt,
+                 wsm);
+}
+
 // filter_out_labels (pado_weighted_unv_unp.h:1052-1184) on pre-filter values;
 // a filtered entry gets bit 15 of its vq slot set.
-__global__ void __launch_bounds__(256) w_filter_kernel(WDev d, const uint32_t *news, uint32_t nnews, uint32_t s)
+__device__ void w_filter_phase(const WDev &d, const uint32_t *news, uint32_t nnews, uint32_t s)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -406,8 +437,13 @@ __global__ void __launch_bounds__(256) w_filter_kernel(WDev d, const uint32_t *n
     }
 }
 
+__global__ void __launch_bounds__(256) w_filter_kernel(WDev d, const uint32_t *news, uint32_t nnews, uint32_t s)
+{
+    w_filter_phase(d, news, nnews, s);
+}
+
 // reset_tables for the roots' buffer rows (pado_weighted_unv_unp.h:872-891).
-__global__ void __launch_bounds__(256) w_buf_reset_kernel(WDev d, uint32_t s, uint32_t nroots)
+__device__ void w_buf_reset_phase(const WDev &d, uint32_t s, uint32_t nroots)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -421,10 +457,15 @@ __global__ void __launch_bounds__(256) w_buf_reset_kernel(WDev d, uint32_t s, ui
     }
 }
 
+__global__ void __launch_bounds__(256) w_buf_reset_kernel(WDev d, uint32_t s, uint32_t nroots)
+{
+    w_buf_reset_phase(d, s, nroots);
+}
+
 // update_index (pado_weighted_unv_unp.h:913-950): append the unfiltered
 // temporary labels in ascending root order, then clear the temporary rows.
-__global__ void __launch_bounds__(256) w_commit_kernel(WDev d, const uint32_t *news, uint32_t nnews, uint32_t s,
-                                                       uint32_t *retry, uint32_t *retry_cnt)
+__device__ void w_commit_phase(const WDev &d, const uint32_t *news, uint32_t nnews, uint32_t s, uint32_t *retry,
+                               uint32_t *retry_cnt)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -474,6 +515,12 @@ __global__ void __launch_bounds__(256) w_commit_kernel(WDev d, const uint32_t *n
     }
 }
 
+__global__ void __launch_bounds__(256) w_commit_kernel(WDev d, const uint32_t *news, uint32_t nnews, uint32_t s,
+                                                       uint32_t *retry, uint32_t *retry_cnt)
+{
+    w_commit_phase(d, news, nnews, s, retry, retry_cnt);
+}
+
 __global__ void __launch_bounds__(256) w_compact_kernel(WDev d, const uint64_t *fin_off, uint32_t *fin_hub,
                                                         int16_t *fin_dist)
 {
@@ -486,6 +533,127 @@ __global__ void __launch_bounds__(256) w_compact_kernel(WDev d, const uint64_t *
             fin_hub[fo + j] = d.pool_hub[base + j];
             fin_dist[fo + j] = d.pool_dist[base + j];
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent loop.  Every block keeps the loop state in registers and derives
+// the same transitions from the same post-barrier counters; the leader saves
+// the state to WLoopCtl only when the launch returns.  Counters are reused by
+// parity and cleared one phase ahead of their next use (see each site).
+// ---------------------------------------------------------------------------
+enum WPhase : uint32_t { WP_START = 0, WP_ROUND = 1, WP_PULL_RETRY = 2, WP_END = 3, WP_COMMIT_RETRY = 4, WP_DONE = 5 };
+enum WExit : uint32_t { WX_RUNNING = 0, WX_DONE = 1, WX_NEED_LOG = 2, WX_NEED_POOL = 3, WX_STALL = 4 };
+
+struct WLoopCtl {
+    GridBar bar;
+    uint32_t phase, b, lid, cur;      // resume point: phase, batch, last stamp, front parity
+    uint32_t rounds, levels;
+    uint32_t front_cnt[2], tails_cnt[2], news_cnt[2];
+    uint32_t rr_cnt, retry_cnt, status, exit_code;
+};
+
+struct WLoopBufs {
+    uint32_t *front[2], *tails[2], *news[2];  // news by batch parity
+    uint32_t *rr, *retry;
+    uint32_t nbatches;
+};
+
+__global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLoopCtl *c, WLoopBufs bf)
+{
+    extern __shared__ __align__(16) unsigned char wsm[];
+    const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+    uint32_t phase = vload(&c->phase), b = vload(&c->b), lid = vload(&c->lid), cur = vload(&c->cur);
+    uint32_t rounds = vload(&c->rounds), levels = vload(&c->levels);
+    auto save = [&](uint32_t ph, uint32_t ex) {
+        if (leader) {
+            c->phase = ph;
+            c->b = b;
+            c->lid = lid;
+            c->cur = cur;
+            c->rounds = rounds;
+            c->levels = levels;
+            c->exit_code = ex;
+        }
+    };
+    for (;;) {
+        if (phase == WP_START) {
+            if (b >= bf.nbatches) {
+                save(WP_DONE, WX_DONE);
+                return;
+            }
+            const uint32_t s = b * d.B, nr = min(d.B, d.n - s);
+            const uint32_t lid0 = lid + 1;
+            cur = lid0 & 1;
+            // front[cur], news[b & 1] and log[lid0 & 1] were cleared at the end of the previous batch
+            w_root_init_phase(d, s, nr, lid0, bf.front[cur], &c->front_cnt[cur], bf.news[b & 1],
+                              &c->news_cnt[b & 1]);
+            if (leader) c->tails_cnt[(lid0 + 1) & 1] = 0;  // the first round's tails
+            if (!grid_barrier(&c->bar, &c->status)) return;
+            lid = lid0;
+            rounds = 0;
+            phase = WP_ROUND;
+            continue;
+        }
+        if (phase == WP_ROUND || phase == WP_PULL_RETRY) {
+            const uint32_t s = b * d.B, nr = min(d.B, d.n - s);
+            const uint32_t lid_cur = lid + 1, nxt = cur ^ 1, tp = lid_cur & 1;
+            if (phase == WP_ROUND) {
+                // Bellman-Ford rounds are bounded by the vertex count
+                if (rounds > d.n + 2) {
+                    save(WP_DONE, WX_STALL);
+                    return;
+                }
+                if (b == 0) w_snap_phase(d, nr);
+                w_mark_phase(d, bf.front[cur], vload(&c->front_cnt[cur]), lid_cur, bf.tails[tp], &c->tails_cnt[tp]);
+                if (leader) d.log_top[lid_cur & 1] = 0;  // last read by the pull of lid_cur - 1
+                if (!grid_barrier(&c->bar, &c->status)) return;
+            }
+            w_pull_phase(d, bf.tails[tp], vload(&c->tails_cnt[tp]), s, b, lid_cur, bf.front[nxt], &c->front_cnt[nxt],
+                         bf.news[b & 1], &c->news_cnt[b & 1], bf.retry, &c->retry_cnt, wsm);
+            if (leader) {
+                c->front_cnt[cur] = 0;             // consumed by this round's mark
+                c->tails_cnt[(lid_cur + 1) & 1] = 0;  // read by the previous round's pull
+            }
+            if (!grid_barrier(&c->bar, &c->status)) return;
+            if (vload(&c->retry_cnt)) {
+                save(WP_PULL_RETRY, WX_NEED_LOG);
+                return;
+            }
+            ++levels;
+            ++rounds;
+            lid = lid_cur;
+            const uint32_t fsize = vload(&c->front_cnt[nxt]);
+            cur = nxt;
+            phase = fsize ? WP_ROUND : WP_END;
+            continue;
+        }
+        if (phase == WP_END || phase == WP_COMMIT_RETRY) {
+            const uint32_t s = b * d.B, nr = min(d.B, d.n - s), nb = b & 1;
+            if (phase == WP_END) {
+                const uint32_t nn = vload(&c->news_cnt[nb]);
+                w_filter_phase(d, bf.news[nb], nn, s);
+                w_buf_reset_phase(d, s, nr);
+                if (leader) {
+                    d.log_top[(lid + 1) & 1] = 0;  // the next batch's root log (read by the last pull)
+                    c->news_cnt[nb ^ 1] = 0;       // the next batch's new-label list
+                }
+                if (!grid_barrier(&c->bar, &c->status)) return;
+                w_commit_phase(d, bf.news[nb], nn, s, bf.retry, &c->retry_cnt);
+            } else {
+                w_commit_phase(d, bf.rr, vload(&c->rr_cnt), s, bf.retry, &c->retry_cnt);
+            }
+            if (!grid_barrier(&c->bar, &c->status)) return;
+            if (vload(&c->retry_cnt)) {
+                save(WP_COMMIT_RETRY, WX_NEED_POOL);
+                return;
+            }
+            ++b;
+            phase = WP_START;
+            continue;
+        }
+        save(WP_DONE, WX_STALL);  // unknown phase
+        return;
     }
 }
 
@@ -625,8 +793,65 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
     PADO_CUDA(cudaEventCreate(&e1));
     PADO_CUDA(cudaEventRecord(e0, s));
     uint32_t lid = 0;
+    const uint32_t nbatches = (uint32_t)(((uint64_t)n + B - 1) / B);
+    const char *loop_env = std::getenv("PADO_LEVEL_LOOP");
+    const bool host_loop = loop_env && !strcmp(loop_env, "host");
     try {
-        for (uint32_t bs = 0, b = 0; bs < n; bs += B, ++b) {
+        PADO_CHECK(nbatches < 65535u, PADO_E_ARG, "more than 65534 batches");
+        if (!host_loop && n) {
+            DBuf<WLoopCtl> ctl(1);
+            DBuf<uint32_t> tails2(n), news2(n), rr(n);
+            ctl.fill_bytes(0, s);
+            WLoopBufs bf{{front0.p, front1.p}, {tails.p, tails2.p}, {news.p, news2.p}, rr.p, retry.p, nbatches};
+            const void *kfn = (const void *)w_loop_kernel;
+            PADO_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pull_smem));
+            int dev = 0, sms = 0, per_sm = 0;
+            PADO_CUDA(cudaGetDevice(&dev));
+            PADO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            PADO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, WPULL_WARPS * 32, pull_smem));
+            PADO_CHECK(per_sm >= 1, PADO_E_CUDA, "weighted labeling loop kernel cannot be resident");
+            const unsigned grid = (unsigned)(sms * std::min(per_sm, 8));
+            PADO_CHECK(grid <= BAR_GROUP * BAR_MAX_GROUPS, PADO_E_CUDA, "grid larger than the barrier supports");
+            WLoopCtl h{};
+            WLoopCtl *cptr = ctl.p;
+            for (int launch = 0;; ++launch) {
+                PADO_CHECK(launch < 512, PADO_E_NOMEM, "round log or label pool could not be grown enough");
+                void *args[] = {&d, &cptr, &bf};
+                PADO_LAUNCH("w_loop_kernel", s,
+                            PADO_CUDA(cudaLaunchCooperativeKernel(kfn, grid, WPULL_WARPS * 32, args, pull_smem, s)));
+                PADO_CUDA(cudaMemcpyAsync(&h, ctl.p, sizeof(WLoopCtl), cudaMemcpyDeviceToHost, s));
+                PADO_CUDA(cudaStreamSynchronize(s));
+                if (h.status & ST_BARRIER_TIMEOUT)
+                    throw Error(PADO_E_TIMEOUT, "weighted labeling loop: a grid barrier timed out");
+                if (h.exit_code == WX_DONE) break;
+                if (h.exit_code == WX_STALL) throw Error(PADO_E_STATE, "relaxation did not converge");
+                if (h.exit_code == WX_NEED_LOG) {
+                    unsigned long long lt[2];
+                    PADO_CUDA(cudaMemcpy(lt, log_top.p, 16, cudaMemcpyDeviceToHost));
+                    grow_logs(lt[(h.lid + 1) & 1]);
+                    // the failed tails become the whole tail list of the round
+                    const uint32_t tp = (h.lid + 1) & 1;
+                    uint32_t *tl[2] = {tails.p, tails2.p};
+                    PADO_CUDA(cudaMemcpyAsync(tl[tp], retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
+                    h.tails_cnt[tp] = h.retry_cnt;
+                } else {
+                    PADO_CHECK(h.exit_code == WX_NEED_POOL, PADO_E_STATE, "weighted labeling loop stopped unexpectedly");
+                    unsigned long long top = 0;
+                    PADO_CUDA(cudaMemcpy(&top, pool_top.p, 8, cudaMemcpyDeviceToHost));
+                    grow_pool(top);
+                    PADO_CUDA(cudaMemcpyAsync(rr.p, retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
+                    h.rr_cnt = h.retry_cnt;
+                }
+                h.retry_cnt = 0;
+                h.status = 0;
+                h.exit_code = WX_RUNNING;
+                PADO_CUDA(cudaMemsetAsync(status.p, 0, 4, s));
+                PADO_CUDA(cudaMemcpyAsync(ctl.p, &h, sizeof(WLoopCtl), cudaMemcpyHostToDevice, s));
+            }
+            run.levels = h.levels;
+            run.batches = nbatches;
+        }
+        for (uint32_t bs = 0, b = 0; host_loop && bs < n; bs += B, ++b) {
             PADO_CHECK(b + 1 < 65536u, PADO_E_ARG, "more than 65534 batches");
             const uint32_t nr = (uint32_t)std::min<uint64_t>(B, (uint64_t)n - bs);
             ++run.batches;
