@@ -149,6 +149,20 @@ def dist_setup(args):
     return world, rank, local
 
 
+def max_over_ranks(pg, values, device):
+    """Each rank labels its own replica; the job takes as long as the slowest
+    rank, so every timing is the maximum over ranks (all_reduce MAX)."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_throughput(labels_per_replica, world, seconds):
+    """Whole-job labels/s of `world` replicas that each label the full graph."""
+    return labels_per_replica * world / seconds
+
+
 def run_reference(args, wl):
     """The reference's own CPU labeling (ParaVertexCentricPLL with all host
     threads when its driver was built here; else the oracle restatement),
@@ -317,9 +331,7 @@ def main():
     dev_mean = statistics.mean(dev_s)
     wall_mean = statistics.mean(wall_s)
     if pg:
-        tt = torch.tensor([dev_mean, wall_mean], device="cuda", dtype=torch.float64)
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        dev_mean, wall_mean = tt.tolist()
+        dev_mean, wall_mean = max_over_ranks(pg, [dev_mean, wall_mean], "cuda")
 
     # ---- queries on the last index (original ids) ----
     idx.order_labels(rank=rk)
@@ -356,11 +368,7 @@ def main():
         prof = read_profile(lib)
         _lib.check(lib.pado_profile(0))
         pidx.close()
-    # the persistent loop kernel runs the mark and pull phases: its algorithmic
-    # bytes are those two counters
-    if "label_loop_kernel" in prof:
-        prof["label_loop_kernel"]["bytes"] = (prof.get("pull_kernel", {}).get("bytes", 0) +
-                                              prof.get("mark_kernel", {}).get("bytes", 0))
+    attribute_loop_bytes(prof)
     peak, peak_src = peaks()
     roofline = None
     label_kernels = {k: v for k, v in prof.items() if not k.startswith("query") and v["launches"]}
@@ -397,7 +405,7 @@ def main():
 
     if grank == 0:
         out = {
-            "metric": METRIC, "value": labels * world / dev_mean, "unit": UNIT, "n_gpus": world,
+            "metric": METRIC, "value": replica_throughput(labels, world, dev_mean), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_mean * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8" if wl["kind"] == "unw" else "int16",
             "data": "synthetic",
@@ -405,7 +413,7 @@ def main():
                        "bp_roots": wl["K"], "batch": wl["B"], "l2": "inputs larger than L2 (graph + label state)",
                        "parallelism": f"replicas x{world}"},
             "labels": labels, "labeling_s": dev_mean, "bp_s": info.bp_seconds, "levels": info.levels,
-            "e2e": {"value": labels * world / wall_mean, "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "e2e": {"value": replica_throughput(labels, world, wall_mean), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "wall_s": wall_mean},
             "queries": {"n": nq, "per_s_device": nq / q_dev_s, "per_s_e2e": nq / q_e2e_s, "roofline": q_roof},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
@@ -508,6 +516,7 @@ def run_many(args):
             ix.close()
         torch.cuda.synchronize()
         prof = read_profile(lib)
+        attribute_loop_bytes(prof)
         _lib.check(lib.pado_profile(0))
     dev_mean, wall_mean = statistics.mean(dev_s), statistics.mean(wall_s)
     out = {
@@ -528,6 +537,16 @@ def run_many(args):
         "clocks": clocks, "gpu_launches": launches, "profile": prof,
     }
     print(json.dumps(out), flush=True)
+
+
+def attribute_loop_bytes(prof):
+    """The persistent loop kernels run the mark and pull phases: their
+    algorithmic bytes are those phases' counters."""
+    for loop, parts in (("label_loop_kernel", ("pull_kernel", "mark_kernel")),
+                        ("many_loop_kernel", ("pull_kernel", "mark_kernel")),
+                        ("w_loop_kernel", ("w_pull_kernel", "w_mark_kernel"))):
+        if loop in prof:
+            prof[loop]["bytes"] = sum(prof.get(k, {}).get("bytes", 0) for k in parts)
 
 
 def read_profile(lib):
