@@ -280,21 +280,51 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
         for (uint32_t i0 = 0; i0 < ntouch; i0 += 32) {
             const uint32_t i = i0 + lane;
             bool acc = false, isnew = false;
+            // check (1), warp-uniform over t's committed labels: a chunk of 32
+            // (hub, distance) pairs is loaded once and broadcast by shuffles,
+            // and each lane still looking gathers 4 buffer entries at a time,
+            // taking the first covering label in list order as the reference.
+            uint32_t c = 0, creal = 0;
+            int32_t m = 0, r = INT_MAX;  // INT_MAX: not a candidate
             if (i < ntouch) {
-                const uint32_t c = touched[i];
-                const int32_t m = rmin[c];
-                int32_t r = INT_MAX;  // INT_MAX: not a candidate
-                if (m < dt_get(d, t, c, stamp)) {
-                    r = INT_MIN;  // accepted unless pruned below
-                    const uint32_t creal = s + c;
-                    const int16_t *brow = d.buf + (uint64_t)c * d.n;
-                    for (uint32_t j = 0; j < clen; ++j) {
-                        const uint32_t hh = d.pool_hub[cbase + j];
-                        const int16_t bb = brow[hh];
-                        if (creal <= hh || bb == I16_INF) continue;
-                        const int32_t val = (int16_t)(d.pool_dist[cbase + j] + bb);
-                        if (val <= m) { r = val; break; }
+                c = touched[i];
+                m = rmin[c];
+                creal = s + c;
+                if (m < dt_get(d, t, c, stamp)) r = INT_MIN;  // accepted unless pruned below
+            }
+            const int16_t *brow = d.buf + (uint64_t)c * d.n;
+            bool look = r == INT_MIN;
+            for (uint32_t j0 = 0; j0 < clen && __any_sync(FULL, look); j0 += 32) {
+                const uint32_t jn = min(32u, clen - j0);
+                const uint32_t hl = lane < (int)jn ? d.pool_hub[cbase + j0 + lane] : 0xffffffffu;
+                const int32_t dl = lane < (int)jn ? (int32_t)d.pool_dist[cbase + j0 + lane] : 0;
+                for (uint32_t k = 0; k < jn; k += 4) {
+                    uint32_t hk[4];
+                    int32_t dk[4], bk[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        hk[u] = __shfl_sync(FULL, hl, (int)(k + u) & 31);
+                        dk[u] = __shfl_sync(FULL, dl, (int)(k + u) & 31);
                     }
+                    if (look) {
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            bk[u] = (k + u < jn && hk[u] < creal) ? (int32_t)brow[hk[u]] : (int32_t)I16_INF;
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            if (look && bk[u] != I16_INF) {
+                                const int32_t val = (int16_t)(dk[u] + bk[u]);
+                                if (val <= m) {
+                                    r = val;
+                                    look = false;
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            if (i < ntouch) {
+                if (r != INT_MAX) {
                     if (r == INT_MIN && b == 0) {
                         const int16_t *crow = d.snap + (uint64_t)c * B;
                         const uint16_t *tq = d.vq + (uint64_t)t * B;
