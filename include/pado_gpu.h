@@ -130,6 +130,67 @@ int pado_w_build(uint32_t n, const uint64_t *off, const uint32_t *adj, const uin
 int pado_w_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w,
                         uint32_t batch, pado_index **out);
 
+/* ---------------------------------------------------------------------------
+ * Graph ingest on the device.
+ *
+ * These replace the reference's host-side graph preparation, run before any
+ * labeler:
+ *   Graph::Graph(const char *) / WeightedGraph::WeightedGraph(const char *)
+ *     (includes/graph.h:95-117, :262-290): "head tail [weight]" text lines,
+ *     lines starting with '#' or '%' skipped;
+ *   Graph::construct (graph.h:125-153; weighted :292-309): both directions
+ *     of every edge stored, duplicates and self-loops kept, n = max id + 1;
+ *   Graph::make_rank (graph.h:156-174): degree descending -- ties broken by
+ *     ascending id here (the reference adds rand()/RAND_MAX, which no two
+ *     hosts reproduce);
+ *   Graph::id_transfer (graph.h:176-206; weighted :367-400): ids relabeled
+ *     to ranks, every list in descending (id, weight) order.
+ * With PADO_INGEST_DEDUPE, self-loops are dropped and repeated undirected
+ * pairs merged first (the first weight in input order wins), the cleaning a
+ * benchmark generator applies to an edge sample.  Edge counts m < 2^31,
+ * fewer than 2^28 vertices.
+ * ------------------------------------------------------------------------- */
+#define PADO_INGEST_DEDUPE 1u
+
+/* Edge list (u[i], v[i]) with optional uint8 weights w[i] (NULL:
+ * unweighted) over ids < n, to the ranked CSR: off[n+1], adj[*entries] (room
+ * for 2m), w_out[*entries] (weighted), and the order rank[n] (rank[v] = new
+ * id of original vertex v).  The output is what pado_unw_build_ranked /
+ * pado_w_build_ranked take, with rank for pado_set_order. */
+int pado_graph_ingest(uint64_t m, const uint32_t *u, const uint32_t *v, const uint8_t *w, uint32_t n,
+                      uint32_t flags, uint64_t *off, uint32_t *adj, uint8_t *w_out, uint32_t *rank,
+                      uint64_t *entries);
+
+/* Same with every array in device memory (the current device): d_adj /
+ * d_w_out need room for 2m entries.  Runs on `stream` (a cudaStream_t; NULL:
+ * the legacy default stream) and returns when the outputs are written. */
+int pado_graph_ingest_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, const uint8_t *d_w, uint32_t n,
+                             uint32_t flags, uint64_t *d_off, uint32_t *d_adj, uint8_t *d_w_out, uint32_t *d_rank,
+                             uint64_t *entries, void *stream);
+
+/* Ingest + labeling in one call, the graph staying on the device between
+ * them: the index answers queries by ORIGINAL id (the reference's sequence
+ * Graph -> make_rank -> id_transfer -> labeler -> order_labels, pado.cpp
+ * main).  n = 0 takes max id + 1. */
+int pado_unw_build_edges(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint32_t flags,
+                         uint32_t bp_roots, uint32_t batch, pado_index **out);
+int pado_w_build_edges(uint64_t m, const uint32_t *u, const uint32_t *v, const uint8_t *w, uint32_t n,
+                       uint32_t flags, uint32_t batch, pado_index **out);
+
+/* Same from an edge-list file (kind PADO_UNWEIGHTED or PADO_WEIGHTED): the
+ * text is read in pieces and parsed on the device.  Lines that are empty,
+ * start with '#' or '%', or do not begin with two decimal ids below 2^32 are
+ * skipped; a missing weight is 0 and weights are cast to uint8 (graph.h:300).
+ * Errors: PADO_E_IO when the file cannot be read. */
+int pado_build_edge_file(const char *path, uint32_t kind, uint32_t flags, uint32_t bp_roots, uint32_t batch,
+                         pado_index **out);
+
+/* The device text parser alone: text[0..bytes) to at most `capacity` edges in
+ * line order; *m receives the edge count (also when it exceeds capacity,
+ * which fails with PADO_E_ARG). */
+int pado_edge_text_parse(const char *text, uint64_t bytes, uint32_t weighted, uint64_t capacity, uint32_t *u,
+                         uint32_t *v, uint8_t *w, uint64_t *m);
+
 /* Install the original-id mapping (rank[v] = rank of original vertex v).
  * Replaces order_labels(rank2id, rank) (pado_unw_unv_unp.h:1227-1310,
  * pado_weighted_unv_unp.h:1715-1779) for indexes built from ranked graphs. */

@@ -83,6 +83,13 @@ def port() -> C.CDLL:
                                        C.POINTER(C.c_uint64), C.POINTER(C.c_double)]
         lib.orc_bfs.argtypes = [C.c_uint32, _u64p, _u32p, C.c_uint32, _u8p]
         lib.orc_dijkstra.argtypes = [C.c_uint32, _u64p, _u32p, _u8p, C.c_uint32, _i32p]
+        lib.orc_graph_ingest.restype = C.c_int
+        lib.orc_graph_ingest.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int,
+                                         _u64p, _u32p, C.c_void_p, _u32p, C.POINTER(C.c_uint64),
+                                         C.POINTER(C.c_uint32)]
+        lib.orc_edge_text_parse.restype = C.c_uint64
+        lib.orc_edge_text_parse.argtypes = [C.c_char_p, C.c_uint64, C.c_int, C.c_uint64, C.c_void_p, C.c_void_p,
+                                            C.c_void_p]
         _port = lib
     return _port
 
@@ -207,8 +214,99 @@ def ref(K: int = 50) -> C.CDLL:
         lib.ref_w_query.restype = C.c_double
         lib.ref_w_query.argtypes = [C.c_uint32, _u64p, _u32p, _i16p, C.c_uint64, _u32p, _u32p,
                                     _i16p, C.c_int]
+        lib.ref_graph_read.restype = C.c_void_p
+        lib.ref_graph_read.argtypes = [C.c_char_p, C.c_int]
+        lib.ref_graph_make.restype = C.c_void_p
+        lib.ref_graph_make.argtypes = [C.c_uint64, _u32p, _u32p, C.c_void_p]
+        lib.ref_graph_n.restype = C.c_uint32
+        lib.ref_graph_n.argtypes = [C.c_void_p]
+        lib.ref_graph_entries.restype = C.c_uint64
+        lib.ref_graph_entries.argtypes = [C.c_void_p]
+        lib.ref_graph_degrees.argtypes = [C.c_void_p, _u32p]
+        lib.ref_graph_transfer.argtypes = [C.c_void_p, _u32p, _u64p, _u32p, C.c_void_p]
+        lib.ref_graph_free.argtypes = [C.c_void_p]
         _refs[K] = lib
     return _refs[K]
+
+
+def _ranked_from_ref(lib, h, weighted: bool):
+    """Degree order with ascending-id ties over the reference Graph's own
+    degrees, then its id_transfer; returns (CSRGraph, rank)."""
+    n = lib.ref_graph_n(h)
+    e = lib.ref_graph_entries(h)
+    deg = np.zeros(max(n, 1), np.uint32)
+    lib.ref_graph_degrees(h, deg)
+    deg = deg[:n]
+    order = np.lexsort((np.arange(n), -deg.astype(np.int64)))
+    rank = np.empty(n, np.uint32)
+    rank[order] = np.arange(n, dtype=np.uint32)
+    off = np.zeros(n + 1, np.uint64)
+    adj = np.zeros(max(e, 1), np.uint32)
+    w = np.zeros(max(e, 1), np.uint8) if weighted else None
+    lib.ref_graph_transfer(h, rank if n else np.zeros(1, np.uint32), off, adj,
+                           None if w is None else w.ctypes.data_as(C.c_void_p))
+    from parallel_distance_oracle_gb300.graphs import CSRGraph
+    return CSRGraph(n, off, adj[:e].copy(), None if w is None else w[:e].copy()), rank
+
+
+def ref_graph_file(path, weighted: bool = False):
+    """The reference reading an edge-list file (Graph(const char *),
+    graph.h:95-117; weighted :262-290) and relabeling it (id_transfer)."""
+    lib = ref(50)
+    h = lib.ref_graph_read(str(path).encode(), int(weighted))
+    try:
+        return _ranked_from_ref(lib, h, weighted)
+    finally:
+        lib.ref_graph_free(h)
+
+
+def ref_graph_edges(u, v, w=None):
+    """The reference's Graph(edge_list) / WeightedGraph(edge_list, weights)
+    (graph.h:125-153, :292-309) followed by id_transfer."""
+    lib = ref(50)
+    u, v = _c(u, np.uint32), _c(v, np.uint32)
+    wc = None if w is None else _c(w, np.uint8)
+    h = lib.ref_graph_make(len(u), u, v, None if wc is None else wc.ctypes.data_as(C.c_void_p))
+    try:
+        return _ranked_from_ref(lib, h, w is not None)
+    finally:
+        lib.ref_graph_free(h)
+
+
+def graph_ingest(u, v, w=None, n: int = 0, dedupe: bool = False):
+    """The restatement of the same preparation (orc_graph_ingest); n = 0
+    takes max id + 1.  Returns (CSRGraph, rank)."""
+    from parallel_distance_oracle_gb300.graphs import CSRGraph
+    lib = port()
+    u, v = _c(u, np.uint32), _c(v, np.uint32)
+    m = len(u)
+    if n == 0 and m:
+        n = int(max(u.max(), v.max())) + 1
+    wc = None if w is None else _c(w, np.uint8)
+    off = np.zeros(n + 1, np.uint64)
+    adj = np.zeros(max(2 * m, 1), np.uint32)
+    wo = np.zeros(max(2 * m, 1), np.uint8) if w is not None else None
+    rank = np.zeros(max(n, 1), np.uint32)
+    ent, nn = C.c_uint64(), C.c_uint32()
+    vp = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    rc = lib.orc_graph_ingest(m, vp(u), vp(v), vp(wc), n, int(dedupe), off, adj, vp(wo), rank, C.byref(ent),
+                              C.byref(nn))
+    if rc != 0:
+        raise ValueError("edge endpoint out of range")
+    e = ent.value
+    return CSRGraph(n, off, adj[:e].copy(), None if wo is None else wo[:e].copy()), rank[:n]
+
+
+def parse_edge_text(text: bytes, weighted: bool = False):
+    """orc_edge_text_parse: (u, v, w) from edge-list text; w None when unweighted."""
+    lib = port()
+    cnt = lib.orc_edge_text_parse(text, len(text), int(weighted), 0, None, None, None)
+    u = np.zeros(max(cnt, 1), np.uint32)
+    v = np.zeros(max(cnt, 1), np.uint32)
+    w = np.zeros(max(cnt, 1), np.uint8) if weighted else None
+    vp = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    lib.orc_edge_text_parse(text, len(text), int(weighted), cnt, vp(u), vp(v), vp(w))
+    return u[:cnt].copy(), v[:cnt].copy(), None if w is None else w[:cnt].copy()
 
 
 def ref_unw_label(g, rank, K: int, B: int, mode: int = 0, threads: int = 1) -> UnwLabels:

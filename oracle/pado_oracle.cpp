@@ -978,4 +978,120 @@ void orc_dijkstra(uint32_t n, const uint64_t *off, const uint32_t *adj, const ui
     for (uint32_t v = 0; v < n; ++v) out[v] = d[v] >= I16_INF - 2 ? I16_INF : (int32_t)d[v];
 }
 
+// ---------------------------------------------------------------------------
+// Graph preparation, the steps the reference runs before any labeler:
+//   Graph::construct (graph.h:125-153; weighted :292-309): both directions of
+//     every edge, duplicates and self-loops kept, n = max id + 1;
+//   make_rank (graph.h:156-174): degree descending, ties by ascending id
+//     (the reference's rand() jitter is not reproducible);
+//   id_transfer (graph.h:176-206; weighted :367-400): relabel to ranks, every
+//     list sorted descending by (id, weight).
+// dedupe != 0 first drops self-loops and keeps the first occurrence (input
+// order, hence its weight) of every undirected pair.  n = 0 takes max id + 1.
+// Returns 0, or -1 when an id is >= n.  adj / w_out need room for 2m.
+// ---------------------------------------------------------------------------
+int orc_graph_ingest(uint64_t m, const uint32_t *u, const uint32_t *v, const uint8_t *w, uint32_t n, int dedupe,
+                     uint64_t *off, uint32_t *adj, uint8_t *w_out, uint32_t *rank, uint64_t *entries,
+                     uint32_t *n_out)
+{
+    if (n == 0)
+        for (uint64_t e = 0; e < m; ++e) n = std::max(n, std::max(u[e], v[e]) + 1);
+    for (uint64_t e = 0; e < m; ++e)
+        if (u[e] >= n || v[e] >= n) return -1;
+    std::vector<uint64_t> keep;  // edge indexes, input order
+    keep.reserve(m);
+    if (dedupe) {
+        std::vector<std::pair<uint64_t, uint64_t>> key;  // ((lo, hi), index)
+        for (uint64_t e = 0; e < m; ++e)
+            if (u[e] != v[e])
+                key.push_back({(uint64_t)std::min(u[e], v[e]) << 32 | std::max(u[e], v[e]), e});
+        std::stable_sort(key.begin(), key.end(),
+                         [](const auto &a, const auto &b) { return a.first < b.first; });
+        for (size_t i = 0; i < key.size(); ++i)
+            if (i == 0 || key[i].first != key[i - 1].first) keep.push_back(key[i].second);
+        std::sort(keep.begin(), keep.end());
+    } else {
+        for (uint64_t e = 0; e < m; ++e) keep.push_back(e);
+    }
+    std::vector<uint32_t> deg(n, 0);
+    for (uint64_t e : keep) {
+        ++deg[u[e]];
+        ++deg[v[e]];
+    }
+    std::vector<uint32_t> order(n);
+    for (uint32_t x = 0; x < n; ++x) order[x] = x;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return deg[a] > deg[b]; });
+    for (uint32_t r = 0; r < n; ++r) rank[order[r]] = r;
+    std::vector<std::vector<std::pair<uint32_t, uint8_t>>> lists(n);
+    for (uint64_t e : keep) {
+        const uint8_t we = w ? w[e] : 0;
+        lists[rank[u[e]]].push_back({rank[v[e]], we});
+        lists[rank[v[e]]].push_back({rank[u[e]], we});
+    }
+    off[0] = 0;
+    for (uint32_t x = 0; x < n; ++x) {
+        std::sort(lists[x].rbegin(), lists[x].rend());
+        for (size_t i = 0; i < lists[x].size(); ++i) {
+            adj[off[x] + i] = lists[x][i].first;
+            if (w_out) w_out[off[x] + i] = lists[x][i].second;
+        }
+        off[x + 1] = off[x] + lists[x].size();
+    }
+    *entries = off[n];
+    *n_out = n;
+    return 0;
+}
+
+// Edge-list text, line by line as Graph(const char *) reads it
+// (graph.h:95-117; weighted :262-290): a line is the bytes before '\n'; it is
+// skipped when empty or when it starts with '#' or '%'.  Otherwise it must
+// begin with two unsigned decimal ids (each after optional blanks -- space,
+// \t, \r, \v, \f -- and an optional '+', at most 2^32 - 1), like
+// `lin >> head >> tail`; a line where that fails is skipped (the reference
+// would repeat the previous line's values).  A weight follows the same rule,
+// is 0 when absent or unparsable and 2^32 - 1 on overflow, and is cast to
+// uint8 (graph.h:300).  Extra columns are ignored.  Returns the number of
+// edges; only the first `cap` are stored.
+uint64_t orc_edge_text_parse(const char *text, uint64_t bytes, int weighted, uint64_t cap, uint32_t *u,
+                             uint32_t *v, uint8_t *w)
+{
+    auto blank = [](char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; };
+    // returns 0 = no number, 1 = number, 2 = number above 2^32 - 1
+    auto number = [&](uint64_t &i, uint64_t end, uint32_t &val) {
+        while (i < end && blank(text[i])) ++i;
+        if (i < end && text[i] == '+') ++i;
+        if (i >= end || text[i] < '0' || text[i] > '9') return 0;
+        uint64_t x = 0;
+        bool over = false;
+        for (; i < end && text[i] >= '0' && text[i] <= '9'; ++i) {
+            x = x * 10 + (uint64_t)(text[i] - '0');
+            if (x > 0xffffffffull) {
+                over = true;
+                x = 0xffffffffull;
+            }
+        }
+        val = (uint32_t)x;
+        return over ? 2 : 1;
+    };
+    uint64_t count = 0, start = 0;
+    while (start < bytes) {
+        uint64_t end = start;
+        while (end < bytes && text[end] != '\n') ++end;
+        uint64_t i = start;
+        uint32_t a = 0, b = 0, c = 0;
+        if (end > start && text[start] != '#' && text[start] != '%' && number(i, end, a) == 1 &&
+            number(i, end, b) == 1) {
+            if (weighted && number(i, end, c) == 0) c = 0;
+            if (count < cap) {
+                u[count] = a;
+                v[count] = b;
+                if (weighted) w[count] = (uint8_t)c;
+            }
+            ++count;
+        }
+        start = end + 1;
+    }
+    return count;
+}
+
 }  // extern "C"

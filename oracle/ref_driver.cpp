@@ -22,6 +22,7 @@
 #include <chrono>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <unordered_map>
 #include <bitset>
 #include <cmath>
@@ -319,6 +320,79 @@ void ref_w_export(void *h, uint64_t *off, uint32_t *hub, int16_t *dist)
     memcpy(dist, r->dist.data(), r->dist.size() * 2);
 }
 void ref_w_free(void *h) { delete (WResult *)h; }
+
+// The reference's graph preparation: Graph(const char *) / Graph(edge_list)
+// (graph.h:95-153) or their weighted forms (graph.h:262-309), the degrees
+// make_rank reads, and id_transfer(rank) (graph.h:176-206, :367-400).
+struct RefGraph {
+    std::unique_ptr<Graph> g;
+    std::unique_ptr<WeightedGraph> wg;
+    idi n() const { return g ? g->num_v : wg->num_v; }
+    idi e() const { return g ? g->num_e : wg->num_e; }
+    const idi *deg() const { return g ? g->out_degrees : wg->out_degrees; }
+};
+
+void *ref_graph_read(const char *path, int weighted)
+{
+    RefGraph *r = new RefGraph;
+    if (weighted)
+        r->wg.reset(new WeightedGraph(path));
+    else
+        r->g.reset(new Graph(path));
+    return r;
+}
+
+void *ref_graph_make(uint64_t m, const uint32_t *u, const uint32_t *v, const uint8_t *w)
+{
+    std::vector<std::pair<idi, idi>> edges(m);
+    for (uint64_t e = 0; e < m; ++e) edges[e] = std::make_pair(u[e], v[e]);
+    RefGraph *r = new RefGraph;
+    if (w) {
+        std::vector<weighti> ws(w, w + m);
+        r->wg.reset(new WeightedGraph(edges, ws));
+    } else {
+        r->g.reset(new Graph(edges));
+    }
+    return r;
+}
+
+uint32_t ref_graph_n(void *h) { return ((RefGraph *)h)->n(); }
+uint64_t ref_graph_entries(void *h) { return ((RefGraph *)h)->e(); }
+void ref_graph_degrees(void *h, uint32_t *deg)
+{
+    RefGraph *r = (RefGraph *)h;
+    memcpy(deg, r->deg(), (size_t)r->n() * 4);
+}
+
+// id_transfer(rank), then the relabeled CSR: off[n+1], adj[entries], w[entries].
+void ref_graph_transfer(void *h, const uint32_t *rank, uint64_t *off, uint32_t *adj, uint8_t *w)
+{
+    RefGraph *r = (RefGraph *)h;
+    const idi n = r->n();
+    std::vector<idi> rk(rank, rank + n);
+    const idi *vert, *deg, *out;
+    if (r->g) {
+        r->g->id_transfer(rk);
+        vert = r->g->vertices;
+        deg = r->g->out_degrees;
+        out = r->g->out_edges;
+    } else {
+        r->wg->id_transfer(rk);
+        vert = r->wg->vertices;
+        deg = r->wg->out_degrees;
+        out = r->wg->out_edges;
+    }
+    off[0] = 0;
+    for (idi x = 0; x < n; ++x) {
+        off[x + 1] = off[x] + deg[x];
+        for (idi k = 0; k < deg[x]; ++k) {
+            adj[off[x] + k] = out[vert[x] + k];
+            if (w && r->wg) w[off[x] + k] = r->wg->out_weights[vert[x] + k];
+        }
+    }
+}
+
+void ref_graph_free(void *h) { delete (RefGraph *)h; }
 
 // The reference's query loop (pado.cpp:105-125 style) over a pair array, on
 // a loaded label set: builds a VertexCentricPLL / WeightedVertexCentricPLL

@@ -15,6 +15,7 @@ from . import build as _build
 PADO_OK = 0
 PADO_UNWEIGHTED = 0
 PADO_WEIGHTED = 1
+PADO_INGEST_DEDUPE = 1
 
 
 class PadoError(RuntimeError):
@@ -57,6 +58,12 @@ def _load() -> C.CDLL:
         "pado_unw_tune_batch": (C.c_int, [u32, vp, vp, vp, vp, u32, vp, u32, u32, P(u32), vp]),
         "pado_w_build": (C.c_int, [u32, vp, vp, vp, vp, u32, P(vp)]),
         "pado_w_build_ranked": (C.c_int, [u32, vp, vp, vp, u32, P(vp)]),
+        "pado_graph_ingest": (C.c_int, [u64, vp, vp, vp, u32, u32, vp, vp, vp, vp, P(u64)]),
+        "pado_graph_ingest_device": (C.c_int, [u64, vp, vp, vp, u32, u32, vp, vp, vp, vp, P(u64), vp]),
+        "pado_unw_build_edges": (C.c_int, [u64, vp, vp, u32, u32, u32, u32, P(vp)]),
+        "pado_w_build_edges": (C.c_int, [u64, vp, vp, vp, u32, u32, u32, P(vp)]),
+        "pado_build_edge_file": (C.c_int, [C.c_char_p, u32, u32, u32, u32, P(vp)]),
+        "pado_edge_text_parse": (C.c_int, [vp, u64, u32, u64, vp, vp, vp, P(u64)]),
         "pado_set_order": (C.c_int, [vp, vp]),
         "pado_free": (None, [vp]),
         "pado_get_info": (C.c_int, [vp, P(Info)]),
@@ -91,7 +98,9 @@ lib = _load()
 EXPORTED = [
     "pado_last_error", "pado_status_string", "pado_version", "pado_unw_build", "pado_unw_build_ranked",
     "pado_unw_build_many", "pado_unw_tune_batch",
-    "pado_w_build", "pado_w_build_ranked", "pado_set_order", "pado_free", "pado_get_info", "pado_export",
+    "pado_w_build", "pado_w_build_ranked", "pado_graph_ingest", "pado_graph_ingest_device",
+    "pado_unw_build_edges", "pado_w_build_edges",
+    "pado_build_edge_file", "pado_edge_text_parse", "pado_set_order", "pado_free", "pado_get_info", "pado_export",
     "pado_import", "pado_query", "pado_query_device", "pado_query_noalloc", "pado_store", "pado_load",
     "pado_kernel_launches", "pado_server_create", "pado_server_add", "pado_server_submit", "pado_server_wait",
     "pado_server_get_stats", "pado_server_replay", "pado_server_destroy",

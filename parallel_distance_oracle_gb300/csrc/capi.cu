@@ -135,36 +135,96 @@ void upload_graph(const pado::HostGraph &hg, pado::DevGraph &g, bool weighted, c
     }
 }
 
+// Builds the labels of a rank-relabeled graph already on the device into h
+// (kind, sizes and, where the input was not ranked, h->rank set by the
+// caller).  `hg` holds the offsets and at least the adjacency of the ids the
+// bit-parallel root selection reads.
+template <typename Phase>
+void label_into(pado_index *h, const pado::HostGraph &hg, const pado::DevGraph &g, uint32_t K, uint32_t B,
+                cudaStream_t s, Phase &&phase)
+{
+    const uint32_t n = hg.n;
+    pado::LabelRun run;
+    if (h->kind == PADO_UNWEIGHTED) {
+        std::vector<uint8_t> used(n, 0);
+        h->bpd.alloc(std::max<uint64_t>((uint64_t)n * K, 1));
+        h->bps.alloc(std::max<uint64_t>((uint64_t)n * K * 2, 1));
+        pado::BpResult bp = pado::bp_label(hg, g, K, used, h->bpd.p, h->bps.p, s);
+        phase("bit-parallel");
+        run = pado::unw_label(g, K, B, used, h->bpd.p, h->bps.p, h->store, s);
+        phase("labeling");
+        h->info.bp_seconds = bp.ms * 1e-3;
+        h->info.build_seconds = (bp.ms + run.ms) * 1e-3;
+        h->info.levels = run.levels + bp.levels;
+    } else {
+        run = pado::w_label(g, B, h->store, s);
+        phase("labeling");
+        h->info.build_seconds = run.ms * 1e-3;
+        h->info.levels = run.levels;
+    }
+    PADO_CUDA(cudaStreamSynchronize(s));
+    h->info.n = n;
+    h->info.kind = h->kind;
+    h->info.bp_roots = h->K;
+    h->info.batch = B;
+    h->info.num_labels = h->store.total;
+    h->info.batches = run.batches;
+    h->info.device_bytes = h->device_bytes();
+}
+
+// PADO_TRACE=1: host phases of a build on stderr.
+struct PhaseTrace {
+    bool on = std::getenv("PADO_TRACE") != nullptr;
+    std::chrono::steady_clock::time_point prev = std::chrono::steady_clock::now();
+    void operator()(const char *what)
+    {
+        if (!on) return;
+        const auto t = std::chrono::steady_clock::now();
+        fprintf(stderr, "build %s %.3f ms\n", what, std::chrono::duration<double, std::milli>(t - prev).count());
+        prev = t;
+    }
+};
+
+struct StreamGuard {
+    cudaStream_t s = nullptr;
+    StreamGuard() { PADO_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+    ~StreamGuard() { cudaStreamDestroy(s); }
+};
+
+void check_build_args(uint32_t K, uint32_t B)
+{
+    PADO_CHECK(B >= 1 && B <= pado::MAX_BATCH, PADO_E_ARG, "batch size must be in [1, 2048]");
+    PADO_CHECK(K <= pado::MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
+}
+
+// Argument checks first: a bad call fails before touching the device.
+std::unique_ptr<pado_index> new_index(bool weighted, uint32_t n, uint32_t K, uint32_t B)
+{
+    check_build_args(K, B);
+    std::unique_ptr<pado_index> h(new pado_index);
+    PADO_CUDA(cudaGetDevice(&h->device));
+    h->kind = weighted ? PADO_WEIGHTED : PADO_UNWEIGHTED;
+    h->n = n;
+    h->K = weighted ? 0 : K;
+    h->B = B;
+    return h;
+}
+
 int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w,
                  const uint32_t *rank, uint32_t K, uint32_t B, pado_index **out)
 {
     if (!out) return fail(PADO_E_ARG, "null output handle");
     *out = nullptr;
     return guarded([&] {
-        // PADO_TRACE=1: host phases of the build on stderr
-        const bool trace = std::getenv("PADO_TRACE") != nullptr;
-        auto t_prev = std::chrono::steady_clock::now();
-        auto phase = [&](const char *what) {
-            if (!trace) return;
-            const auto t = std::chrono::steady_clock::now();
-            fprintf(stderr, "build %s %.3f ms\n", what, std::chrono::duration<double, std::milli>(t - t_prev).count());
-            t_prev = t;
-        };
-        PADO_CHECK(B >= 1 && B <= pado::MAX_BATCH, PADO_E_ARG, "batch size must be in [1, 2048]");
-        PADO_CHECK(K <= pado::MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
+        PhaseTrace phase;
+        check_build_args(K, B);
         PADO_CHECK(!weighted || w != nullptr || (off && off[n] == 0), PADO_E_ARG, "null weights");
         check_graph(n, off, adj);
         phase("check");
         if (rank) check_rank(n, rank);
-        std::unique_ptr<pado_index> h(new pado_index);
-        PADO_CUDA(cudaGetDevice(&h->device));
-        h->kind = weighted ? PADO_WEIGHTED : PADO_UNWEIGHTED;
-        h->n = n;
-        h->K = weighted ? 0 : K;
-        h->B = B;
-        cudaStream_t s;
-        PADO_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-        struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
+        std::unique_ptr<pado_index> h = new_index(weighted, n, K, B);
+        StreamGuard sg;
+        const cudaStream_t s = sg.s;
         pado::HostGraph hg = pado::relabel_host(n, off, adj, weighted ? w : nullptr, rank);
         phase("relabel");
         pado::DevGraph g;
@@ -173,35 +233,44 @@ int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t 
             h->rank.alloc(std::max<uint32_t>(n, 1));
             h->rank.upload(rank, n, s);
         }
-        if (trace) PADO_CUDA(cudaStreamSynchronize(s));
+        if (phase.on) PADO_CUDA(cudaStreamSynchronize(s));
         phase("upload");
-        pado::LabelRun run;
-        if (!weighted) {
-            std::vector<uint8_t> used(n, 0);
-            h->bpd.alloc(std::max<uint64_t>((uint64_t)n * K, 1));
-            h->bps.alloc(std::max<uint64_t>((uint64_t)n * K * 2, 1));
-            pado::BpResult bp = pado::bp_label(hg, g, K, used, h->bpd.p, h->bps.p, s);
-            phase("bit-parallel");
-            run = pado::unw_label(g, K, B, used, h->bpd.p, h->bps.p, h->store, s);
-            phase("labeling");
-            h->info.bp_seconds = bp.ms * 1e-3;
-            h->info.build_seconds = (bp.ms + run.ms) * 1e-3;
-            h->info.levels = run.levels + bp.levels;
-        } else {
-            run = pado::w_label(g, B, h->store, s);
-            h->info.build_seconds = run.ms * 1e-3;
-            h->info.levels = run.levels;
-        }
-        PADO_CUDA(cudaStreamSynchronize(s));
-        h->info.n = n;
-        h->info.kind = h->kind;
-        h->info.bp_roots = h->K;
-        h->info.batch = B;
-        h->info.num_labels = h->store.total;
-        h->info.batches = run.batches;
-        h->info.device_bytes = h->device_bytes();
+        label_into(h.get(), hg, g, h->K, B, s, phase);
         *out = h.release();
     });
+}
+
+// Labels the graph that ingest_edges made (ranked CSR on the device) and
+// installs its order, so queries take original ids.
+void build_ingested(pado_index *h, pado::IngestResult &r, uint32_t K, uint32_t B, cudaStream_t s, PhaseTrace &phase)
+{
+    const uint32_t n = r.n;
+    h->n = n;
+    PADO_CHECK(n < 0xffffffffu, PADO_E_ARG, "too many vertices");
+    pado::DevGraph g;
+    g.n = n;
+    g.m = r.m;
+    g.off.alloc((uint64_t)n + 1);
+    g.off.upload(r.off.data(), (uint64_t)n + 1, s);
+    g.adj = std::move(r.adj);
+    g.w = std::move(r.w);
+    // Root selection reads the lists of the first roots and their neighbours
+    // only: root i is the smallest id no earlier root or selected neighbour
+    // took, so every root id is below 65 * K.  Only that prefix of the
+    // adjacency comes to the host.
+    pado::HostGraph hg;
+    hg.n = n;
+    hg.off = std::move(r.off);
+    if (h->kind == PADO_UNWEIGHTED && h->K) {
+        const uint32_t R = (uint32_t)std::min<uint64_t>(n, 65ull * h->K);
+        hg.adj.resize(hg.off[R]);
+        g.adj.download(hg.adj.data(), hg.off[R], s);
+    }
+    h->rank.alloc(std::max<uint32_t>(n, 1));
+    h->rank.upload(r.rank.data(), n, s);
+    PADO_CUDA(cudaStreamSynchronize(s));
+    phase("upload");
+    label_into(h, hg, g, h->K, B, s, phase);
 }
 
 // Export in original-id order: vertex v takes the list (and BP row) of rank[v].
@@ -484,6 +553,151 @@ int pado_w_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, co
                         pado_index **out)
 {
     return build_common(true, n, off, adj, w, nullptr, 0, batch, out);
+}
+
+int pado_graph_ingest(uint64_t m, const uint32_t *u, const uint32_t *v, const uint8_t *w, uint32_t n, uint32_t flags,
+                      uint64_t *off, uint32_t *adj, uint8_t *w_out, uint32_t *rank, uint64_t *entries)
+{
+    return guarded([&] {
+        PADO_CHECK((flags & ~(uint32_t)PADO_INGEST_DEDUPE) == 0, PADO_E_ARG, "unknown ingest flags");
+        PADO_CHECK(m == 0 || (u && v), PADO_E_ARG, "null edge arrays");
+        PADO_CHECK(n > 0 || m == 0, PADO_E_ARG, "n must be given (more than the largest id)");
+        PADO_CHECK(off && rank && entries && (m == 0 || adj), PADO_E_ARG, "null output array");
+        PADO_CHECK(!w || w_out || m == 0, PADO_E_ARG, "null weight output");
+        StreamGuard sg;
+        const cudaStream_t s = sg.s;
+        pado::DBuf<uint32_t> du(std::max<uint64_t>(m, 1)), dv(std::max<uint64_t>(m, 1));
+        pado::DBuf<uint8_t> dw(w ? std::max<uint64_t>(m, 1) : 0);
+        du.upload(u, m, s);
+        dv.upload(v, m, s);
+        if (w) dw.upload(w, m, s);
+        pado::IngestResult r = pado::ingest_edges(m, du.p, dv.p, w ? dw.p : nullptr, n, flags & PADO_INGEST_DEDUPE, s);
+        r.adj.download(adj, r.m, s);
+        if (w) r.w.download(w_out, r.m, s);
+        for (uint64_t k = 0; k <= n; ++k) off[k] = r.off[k];
+        std::memcpy(rank, r.rank.data(), (uint64_t)n * sizeof(uint32_t));
+        PADO_CUDA(cudaStreamSynchronize(s));
+        *entries = r.m;
+    });
+}
+
+int pado_graph_ingest_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, const uint8_t *d_w, uint32_t n,
+                             uint32_t flags, uint64_t *d_off, uint32_t *d_adj, uint8_t *d_w_out, uint32_t *d_rank,
+                             uint64_t *entries, void *stream)
+{
+    return guarded([&] {
+        PADO_CHECK((flags & ~(uint32_t)PADO_INGEST_DEDUPE) == 0, PADO_E_ARG, "unknown ingest flags");
+        PADO_CHECK(m == 0 || (d_u && d_v), PADO_E_ARG, "null edge arrays");
+        PADO_CHECK(n > 0 || m == 0, PADO_E_ARG, "n must be given (more than the largest id)");
+        PADO_CHECK(d_off && d_rank && entries && (m == 0 || d_adj), PADO_E_ARG, "null output array");
+        PADO_CHECK(!d_w || d_w_out || m == 0, PADO_E_ARG, "null weight output");
+        const cudaStream_t s = (cudaStream_t)stream;
+        pado::IngestResult r = pado::ingest_edges(m, d_u, d_v, d_w, n, flags & PADO_INGEST_DEDUPE, s, d_adj, d_w_out);
+        std::vector<uint64_t> off64(r.off.begin(), r.off.end());
+        PADO_CUDA(cudaMemcpyAsync(d_off, off64.data(), off64.size() * 8, cudaMemcpyHostToDevice, s));
+        PADO_CUDA(cudaMemcpyAsync(d_rank, r.rank.data(), (uint64_t)n * 4, cudaMemcpyHostToDevice, s));
+        PADO_CUDA(cudaStreamSynchronize(s));
+        *entries = r.m;
+    });
+}
+
+namespace {
+int edges_build(bool weighted, uint64_t m, const uint32_t *u, const uint32_t *v, const uint8_t *w, uint32_t n,
+                uint32_t flags, uint32_t K, uint32_t B, pado_index **out)
+{
+    if (!out) return fail(PADO_E_ARG, "null output handle");
+    *out = nullptr;
+    return guarded([&] {
+        PhaseTrace phase;
+        PADO_CHECK((flags & ~(uint32_t)PADO_INGEST_DEDUPE) == 0, PADO_E_ARG, "unknown ingest flags");
+        PADO_CHECK(m == 0 || (u && v), PADO_E_ARG, "null edge arrays");
+        PADO_CHECK(!weighted || w || m == 0, PADO_E_ARG, "null weights");
+        std::unique_ptr<pado_index> h = new_index(weighted, n, K, B);
+        StreamGuard sg;
+        const cudaStream_t s = sg.s;
+        pado::IngestResult r;
+        {
+            pado::DBuf<uint32_t> du(std::max<uint64_t>(m, 1)), dv(std::max<uint64_t>(m, 1));
+            pado::DBuf<uint8_t> dw(weighted ? std::max<uint64_t>(m, 1) : 0);
+            du.upload(u, m, s);
+            dv.upload(v, m, s);
+            if (weighted) dw.upload(w, m, s);
+            r = pado::ingest_edges(m, du.p, dv.p, weighted ? dw.p : nullptr, n, flags & PADO_INGEST_DEDUPE, s);
+        }
+        phase("ingest");
+        build_ingested(h.get(), r, h->K, B, s, phase);
+        *out = h.release();
+    });
+}
+}  // namespace
+
+int pado_unw_build_edges(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint32_t flags,
+                         uint32_t bp_roots, uint32_t batch, pado_index **out)
+{
+    return edges_build(false, m, u, v, nullptr, n, flags, bp_roots, batch, out);
+}
+
+int pado_w_build_edges(uint64_t m, const uint32_t *u, const uint32_t *v, const uint8_t *w, uint32_t n,
+                       uint32_t flags, uint32_t batch, pado_index **out)
+{
+    return edges_build(true, m, u, v, w, n, flags, 0, batch, out);
+}
+
+int pado_build_edge_file(const char *path, uint32_t kind, uint32_t flags, uint32_t bp_roots, uint32_t batch,
+                         pado_index **out)
+{
+    if (!out) return fail(PADO_E_ARG, "null output handle");
+    *out = nullptr;
+    return guarded([&] {
+        PhaseTrace phase;
+        PADO_CHECK(kind == PADO_UNWEIGHTED || kind == PADO_WEIGHTED, PADO_E_ARG, "unknown index kind");
+        PADO_CHECK((flags & ~(uint32_t)PADO_INGEST_DEDUPE) == 0, PADO_E_ARG, "unknown ingest flags");
+        const bool weighted = kind == PADO_WEIGHTED;
+        std::unique_ptr<pado_index> h = new_index(weighted, 0, bp_roots, batch);
+        StreamGuard sg;
+        const cudaStream_t s = sg.s;
+        pado::IngestResult r;
+        {
+            pado::EdgeTextParser p = pado::read_edge_file(path, weighted, s);
+            phase("read+parse");
+            r = pado::ingest_edges(p.m, p.u.p, p.v.p, weighted ? p.w.p : nullptr, 0, flags & PADO_INGEST_DEDUPE, s);
+        }
+        phase("ingest");
+        build_ingested(h.get(), r, h->K, batch, s, phase);
+        *out = h.release();
+    });
+}
+
+int pado_edge_text_parse(const char *text, uint64_t bytes, uint32_t weighted, uint64_t capacity, uint32_t *u,
+                         uint32_t *v, uint8_t *w, uint64_t *m)
+{
+    return guarded([&] {
+        PADO_CHECK(m != nullptr, PADO_E_ARG, "null edge count");
+        *m = 0;
+        PADO_CHECK(bytes == 0 || text, PADO_E_ARG, "null text");
+        PADO_CHECK(capacity == 0 || (u && v && (!weighted || w)), PADO_E_ARG, "null output array");
+        StreamGuard sg;
+        pado::EdgeTextParser p(weighted != 0, std::min<uint64_t>(pado::edge_bound_for_text(bytes), (1ull << 32) - 1),
+                               sg.s);
+        // pieces of at most 1 GiB, each ending at a line end
+        const uint64_t piece = pado::text_piece_bytes(1ull << 30);
+        uint64_t at = 0;
+        while (at < bytes) {
+            uint64_t end = std::min(bytes, at + piece);
+            if (end < bytes) {
+                while (end > at && text[end - 1] != '\n') --end;
+                PADO_CHECK(end > at, PADO_E_ARG, "a line longer than the parse piece (1 GiB)");
+            }
+            p.feed(text + at, end - at);
+            at = end;
+        }
+        *m = p.m;
+        PADO_CHECK(p.m <= capacity, PADO_E_ARG, "more edges than the output capacity (*m holds the count)");
+        p.u.download(u, p.m, sg.s);
+        p.v.download(v, p.m, sg.s);
+        if (weighted) p.w.download(w, p.m, sg.s);
+        PADO_CUDA(cudaStreamSynchronize(sg.s));
+    });
 }
 
 int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *off, const uint32_t *const *adj,

@@ -108,6 +108,46 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
 // weighted.cu: batched pruned relaxation (pado_weighted_unv_unp.h:281-1526).
 LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s);
 
+// ingest.cu: an undirected edge list (device arrays, original ids) to the
+// ranked CSR: Graph::construct + make_rank + id_transfer (graph.h:125-206)
+// with degree ties broken by ascending id.  n = 0 takes max id + 1; dedupe
+// drops self-loops and merges repeated pairs (first weight wins) first.  The
+// adjacency (and weights) go to adj_out / w_out (device, room for 2m) when
+// given, else into the result's own buffers.
+struct IngestResult {
+    uint32_t n = 0;
+    uint64_t m = 0;                  // directed entries
+    std::vector<uint32_t> rank;      // original id -> rank
+    std::vector<uint32_t> off;       // n + 1, rank-indexed
+    DBuf<uint32_t> adj;              // m: rank ids, every list descending (id, weight)
+    DBuf<uint8_t> w;                 // m (weighted only)
+};
+IngestResult ingest_edges(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, const uint8_t *d_w, uint32_t n,
+                          bool dedupe, cudaStream_t s, uint32_t *adj_out = nullptr, uint8_t *w_out = nullptr);
+
+// Edge-list text ("head tail [weight]" lines, graph.h:95-117, :262-290)
+// parsed on the device into u / v / w (device, m edges so far, in line
+// order).  feed() takes whole lines; every call completes before returning.
+class EdgeTextParser {
+public:
+    EdgeTextParser(bool weighted, uint64_t max_edges, cudaStream_t s);
+    void feed(const char *text, uint64_t bytes);
+    uint64_t m = 0;
+    DBuf<uint32_t> u, v;
+    DBuf<uint8_t> w;
+
+private:
+    bool weighted_;
+    cudaStream_t s_;
+    uint64_t cap_ = 0;
+    DBuf<uint8_t> text_;
+    DBuf<uint32_t> cnt_, nl_, ok_, lu_, lv_;
+    DBuf<uint8_t> lw_;
+};
+uint64_t edge_bound_for_text(uint64_t bytes);
+uint64_t text_piece_bytes(uint64_t dflt);
+EdgeTextParser read_edge_file(const char *path, bool weighted, cudaStream_t s);
+
 // capi.cu: the calling thread's last-error message, and read-only access to
 // an index handle, for entry points defined in other files.
 int set_error(int code, const std::string &msg);

@@ -76,6 +76,13 @@ def rmat(scale: int, edge_factor: int, seed: int, a: float = 0.57, b: float = 0.
     the result symmetrised and deduplicated; isolated vertices are kept.  With
     ``weights=(lo, hi)``, each undirected edge gets a uniform integer weight in
     [lo, hi] drawn from the same stream after the structure."""
+    return csr_from_edges(*rmat_edges(scale, edge_factor, seed, a, b, c, weights))
+
+
+def rmat_edges(scale: int, edge_factor: int, seed: int, a: float = 0.57, b: float = 0.19,
+               c: float = 0.19, weights: tuple[int, int] | None = None):
+    """The raw samples behind :func:`rmat`, before cleaning: ``(n, u, v, w)``
+    with self-loops and repeats still in (``w`` None without weights)."""
     n = 1 << scale
     m = n * edge_factor
     rng = _rng(seed)
@@ -91,7 +98,7 @@ def rmat(scale: int, edge_factor: int, seed: int, a: float = 0.57, b: float = 0.
     w = None
     if weights is not None:
         w = rng.integers(weights[0], weights[1] + 1, size=m, dtype=np.int64).astype(np.uint8)
-    return csr_from_edges(n, u, v, w)
+    return n, u, v, w
 
 
 def erdos_renyi(n: int, avg_degree: float, seed: int) -> CSRGraph:

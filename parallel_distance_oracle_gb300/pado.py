@@ -169,6 +169,35 @@ class VertexCentricPLL(_Index):
         self._h = h
 
     @classmethod
+    def from_edges(cls, u, v, n: int | None = None, dedupe: bool = False, bp_roots: int = 50,
+                   batch: int = 1024) -> "VertexCentricPLL":
+        """Edge list in, labels out, queries by original id: the reference's
+        Graph -> make_rank -> id_transfer -> labeler -> order_labels sequence
+        (pado.cpp main), with the graph prepared on the device
+        (pado_unw_build_edges).  ``n=None`` takes max id + 1."""
+        obj = cls(bp_roots=bp_roots, batch=batch)
+        u, v = _u32(u), _u32(v)
+        if len(u) != len(v):
+            raise ValueError("u and v differ in length")
+        h = C.c_void_p()
+        check(lib.pado_unw_build_edges(len(u), ptr(u), ptr(v), n or 0, _lib.PADO_INGEST_DEDUPE if dedupe else 0,
+                                       bp_roots, batch, C.byref(h)))
+        obj._h = h
+        return obj
+
+    @classmethod
+    def from_edge_file(cls, path: str, dedupe: bool = False, bp_roots: int = 50,
+                       batch: int = 1024) -> "VertexCentricPLL":
+        """Graph(filename) (graph.h:95-117) through labeling, parsed and
+        prepared on the device (pado_build_edge_file)."""
+        obj = cls(bp_roots=bp_roots, batch=batch)
+        h = C.c_void_p()
+        check(lib.pado_build_edge_file(str(path).encode(), PADO_UNWEIGHTED,
+                                       _lib.PADO_INGEST_DEDUPE if dedupe else 0, bp_roots, batch, C.byref(h)))
+        obj._h = h
+        return obj
+
+    @classmethod
     def from_labels(cls, labels: CanonicalLabels) -> "VertexCentricPLL":
         """Query-only index from canonical arrays (e.g. the reference's labels)."""
         obj = cls()
@@ -363,6 +392,32 @@ class WeightedVertexCentricPLL(_Index):
         self._h = h
 
     @classmethod
+    def from_edges(cls, u, v, w, n: int | None = None, dedupe: bool = False,
+                   batch: int = 512) -> "WeightedVertexCentricPLL":
+        """Weighted edge list in, labels out, queries by original id
+        (pado_w_build_edges); weights are uint8 as WeightedGraph stores them."""
+        obj = cls(batch=batch)
+        u, v, w = _u32(u), _u32(v), np.ascontiguousarray(w, np.uint8)
+        if not (len(u) == len(v) == len(w)):
+            raise ValueError("u, v and w differ in length")
+        h = C.c_void_p()
+        check(lib.pado_w_build_edges(len(u), ptr(u), ptr(v), ptr(w), n or 0,
+                                     _lib.PADO_INGEST_DEDUPE if dedupe else 0, batch, C.byref(h)))
+        obj._h = h
+        return obj
+
+    @classmethod
+    def from_edge_file(cls, path: str, dedupe: bool = False, batch: int = 512) -> "WeightedVertexCentricPLL":
+        """WeightedGraph(filename) (graph.h:262-290) through labeling, on the
+        device (pado_build_edge_file)."""
+        obj = cls(batch=batch)
+        h = C.c_void_p()
+        check(lib.pado_build_edge_file(str(path).encode(), PADO_WEIGHTED, _lib.PADO_INGEST_DEDUPE if dedupe else 0,
+                                       0, batch, C.byref(h)))
+        obj._h = h
+        return obj
+
+    @classmethod
     def from_labels(cls, labels: CanonicalLabels) -> "WeightedVertexCentricPLL":
         obj = cls()
         h = C.c_void_p()
@@ -374,6 +429,44 @@ class WeightedVertexCentricPLL(_Index):
 
 
 WeightedParaVertexCentricPLL = WeightedVertexCentricPLL
+
+
+def graph_ingest(u, v, w=None, n: int | None = None, dedupe: bool = False):
+    """Edge list (original ids) to the rank-relabeled CSR the labelers take,
+    on the device (pado_graph_ingest): Graph::construct + make_rank +
+    id_transfer (graph.h:125-206), degree ties by ascending id.  Returns
+    ``(G_ranked, rank)``; ``rank[v]`` is the new id of vertex ``v``."""
+    u, v = _u32(u), _u32(v)
+    if len(u) != len(v) or (w is not None and len(w) != len(u)):
+        raise ValueError("edge arrays differ in length")
+    m = len(u)
+    if n is None:
+        n = int(max(u.max(initial=0), v.max(initial=0))) + 1 if m else 0
+    wi = None if w is None else np.ascontiguousarray(w, np.uint8)
+    off = np.zeros(n + 1, np.uint64)
+    adj = np.zeros(max(2 * m, 1), np.uint32)
+    wo = np.zeros(max(2 * m, 1), np.uint8) if wi is not None else None
+    rank = np.zeros(max(n, 1), np.uint32)
+    entries = C.c_uint64()
+    check(lib.pado_graph_ingest(m, ptr(u), ptr(v), ptr(wi), n, _lib.PADO_INGEST_DEDUPE if dedupe else 0, ptr(off),
+                                ptr(adj), ptr(wo), ptr(rank), C.byref(entries)))
+    e = entries.value
+    return CSRGraph(n, off, adj[:e].copy(), None if wo is None else wo[:e].copy()), rank[:n]
+
+
+def parse_edge_text(text: bytes, weighted: bool = False):
+    """Edge-list text to arrays on the device (pado_edge_text_parse), with the
+    line rules of Graph(filename) (graph.h:95-117): returns ``(u, v, w)``,
+    ``w`` None when unweighted."""
+    buf = np.frombuffer(text, np.uint8) if len(text) else np.zeros(1, np.uint8)
+    cap = len(text) // 4 + 1
+    u = np.zeros(cap, np.uint32)
+    v = np.zeros(cap, np.uint32)
+    w = np.zeros(cap, np.uint8) if weighted else None
+    m = C.c_uint64()
+    check(lib.pado_edge_text_parse(ptr(buf), len(text), int(weighted), cap, ptr(u), ptr(v), ptr(w), C.byref(m)))
+    k = m.value
+    return u[:k].copy(), v[:k].copy(), None if w is None else w[:k].copy()
 
 
 def version() -> str:

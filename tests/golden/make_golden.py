@@ -78,7 +78,7 @@ def w_case(name, g, B, seed):
 
 
 def main():
-    for p in HERE.glob("*.npz"):
+    for p in list(HERE.glob("unw_*.npz")) + list(HERE.glob("w_*.npz")):
         p.unlink()
     tools = REF / "tools"
     # the reference's own fixture graphs
