@@ -3,7 +3,7 @@
 synthetic graph plus exact distance queries, against the reference's CPU code.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload rmat20|rmat14|wrmat18]
+                    [--workload rmat20|rmat14|rmat18|wrmat18|many|serve|ingest]
 
 A step labels the whole graph once (bit-parallel rows + every root batch).
 ``value`` is canonical labels per second of device labeling time (inputs
@@ -60,6 +60,12 @@ MANY = dict(graphs=512, n_lo=1000, n_hi=20000, er_degree=6, grid_frac=0.02, K=50
 # log-uniform in [1, 65536], endpoints Zipf(1.1) over degree rank.
 SERVE = dict(budget=40 << 30, graphs=64, kmax=65536, zipf=1.1, rates=(1e4, 3e4, 5e4, 1e5, 1.5e5, 2e5, 3e5, 1e6, 1e7),
              pairs_per_rate=40_000_000, max_batch_pairs=1 << 18, slots=8, seed=9)
+# Graph ingest: the raw samples of the R-MAT s20/ef16 generator (16.8M
+# edges, repeats and self-loops kept as the reference's Graph keeps them,
+# n = max id + 1) to the rank-relabeled CSR with its vertex order.  The CPU
+# side is the reference's Graph(edge_list) + id_transfer on the s18 samples.
+INGEST = dict(scale=20, ef=16, seed=2, ref_scale=18, scratch_cache=2 << 30,
+              desc="raw R-MAT s20 ef16 samples -> Graph::construct + degree rank + id_transfer (no dedupe)")
 METRIC = "labels_per_s"
 UNIT = "labels/s"
 
@@ -221,7 +227,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + ["many", "serve"])
+    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + ["many", "serve", "ingest"])
     ap.add_argument("--many-graphs", type=int, default=MANY["graphs"])
     ap.add_argument("--many-nmax", type=int, default=MANY["n_hi"])
     ap.add_argument("--many-batch", type=int, default=0, help="skip tuning and use this batch size")
@@ -230,11 +236,15 @@ def main():
     ap.add_argument("--ref-batches", type=int, default=None,
                     help="root batches in one CPU-baseline sample (default: per workload)")
     ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--ingest-scale", type=int, default=INGEST["scale"],
+                    help="R-MAT scale of the ingest workload's samples (smaller for ncu captures)")
     args = ap.parse_args()
     if args.workload == "many":
         return run_many(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "ingest":
+        return run_ingest(args)
     wl = WORKLOADS[args.workload]
     if args.ref_batches is None:
         args.ref_batches = wl["ref_batches"]
@@ -537,6 +547,177 @@ def run_many(args):
         "clocks": clocks, "gpu_launches": launches, "profile": prof,
     }
     print(json.dumps(out), flush=True)
+
+
+def ingest_edges_sample(scale: int):
+    n, u, v, _ = G.rmat_edges(scale, INGEST["ef"], INGEST["seed"])
+    u, v = u.astype(np.uint32), v.astype(np.uint32)
+    return int(max(u.max(), v.max())) + 1, u, v
+
+
+def ingest_cpu(scale: int):
+    """The reference's Graph(edge_list) + degree order + id_transfer on the
+    raw samples at `scale` (the oracle restatement where the reference driver
+    is absent); returns (edges/s, seconds, kind)."""
+    from oracle import orc
+    n, u, v = ingest_edges_sample(scale)
+    have_ref = orc.ref_available(50)
+    if have_ref:
+        orc.ref(50)  # load (or build) the driver outside the timed call
+    t0 = time.perf_counter()
+    if have_ref:
+        orc.ref_graph_edges(u, v)
+        kind = "reference"
+    else:
+        orc.graph_ingest(u, v)
+        kind = "port"
+    sec = time.perf_counter() - t0
+    return len(u) / sec, sec, kind, len(u)
+
+
+# Algorithmic bytes of one launch of the ingest kernels, L = directed entries
+# (2 per edge), m = edges: the keys each radix pass reads and writes, the
+# keys' build from the edge list and the adjacency read out of them.
+def ingest_kernel_bytes(kernel: str, m: int):
+    L = 2 * m
+    return {"rs_scatter_kernel": 16 * L, "rs_hist_kernel": 8 * L, "entry_key_kernel": 8 * m + 8 * m + 8 * L,
+            "extract_kernel": 12 * L, "degree_kernel": 8 * m + 16 * m}.get(kernel)
+
+
+def run_ingest(args):
+    """Edge list -> ranked CSR on the device.  value = input edges/s with the
+    edge arrays resident in HBM (pado_graph_ingest_device, CUDA events);
+    e2e = the same through pado_graph_ingest from pinned host arrays to host
+    CSR, wall clock."""
+    world, grank, local = dist_setup(args)
+    if args.impl == "reference":
+        if grank != 0:
+            return
+        vals, secs, kind, m = [], [], None, 0
+        for i in range(args.warmup + args.steps):
+            v, sec, kind, m = ingest_cpu(INGEST["ref_scale"])
+            if i >= args.warmup:
+                vals.append(v)
+                secs.append(sec)
+            log(f"reference step {i}: {m} edges in {sec:.2f}s ({kind})")
+        v = statistics.mean(vals)
+        sample = f"raw R-MAT s{INGEST['ref_scale']} ef16 samples ({m} edges) per step"
+        print(json.dumps({"metric": "edges_per_s", "value": v, "unit": "edges/s", "impl": "reference",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": statistics.mean(secs) * 1e3, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                          "config": {"workload": "ingest", "desc": INGEST["desc"]},
+                          "cpu_baseline": {"value": v, "unit": "edges/s", "cores": 1, "kind": kind, "sample": sample},
+                          "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    from parallel_distance_oracle_gb300 import _lib
+    lib = _lib.lib
+    n, u, v = ingest_edges_sample(args.ingest_scale)
+    m = len(u)
+    log(f"ingest: {m} edges, n = {n}")
+    du = torch.from_numpy(u.view(np.int32)).cuda()
+    dv = torch.from_numpy(v.view(np.int32)).cuda()
+    d_off = torch.empty(n + 1, dtype=torch.int64, device="cuda")
+    d_adj = torch.empty(2 * m, dtype=torch.int32, device="cuda")
+    d_rank = torch.empty(n, dtype=torch.int32, device="cuda")
+    hu = torch.from_numpy(u.view(np.int32)).pin_memory()
+    hv = torch.from_numpy(v.view(np.int32)).pin_memory()
+    h_off = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    h_adj = torch.empty(2 * m, dtype=torch.int32).pin_memory()
+    h_rank = torch.empty(n, dtype=torch.int32).pin_memory()
+    stream = torch.cuda.current_stream()
+    ent = C.c_uint64()
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def dev_once():
+        _lib.check(lib.pado_graph_ingest_device(m, P(du), P(dv), None, n, 0, P(d_off), P(d_adj), None, P(d_rank),
+                                                C.byref(ent), C.c_void_p(stream.cuda_stream)))
+
+    def host_once():
+        _lib.check(lib.pado_graph_ingest(m, P(hu), P(hv), None, n, 0, P(h_off), P(h_adj), None, P(h_rank),
+                                         C.byref(ent)))
+
+    # a service ingesting graph after graph keeps the sort scratch reserved
+    _lib.check(lib.pado_set_scratch_cache(INGEST["scratch_cache"]))
+    for _ in range(args.warmup):
+        dev_once()
+        host_once()
+    assert ent.value == 2 * m
+    torch.cuda.synchronize()
+    assert torch.equal(d_adj.cpu(), h_adj) and torch.equal(d_off.cpu(), h_off) and torch.equal(d_rank.cpu(), h_rank)
+    launches0 = lib.pado_kernel_launches()
+    dev_s, wall_s = [], []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            torch.cuda.synchronize()
+            e0.record(stream)
+            dev_once()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            dev_s.append(e0.elapsed_time(e1) / 1e3)
+            t0 = time.perf_counter()
+            host_once()
+            wall_s.append(time.perf_counter() - t0)
+            log(f"step {i}: device-resident {dev_s[-1] * 1e3:.2f} ms, host arrays {wall_s[-1] * 1e3:.2f} ms")
+    launches = lib.pado_kernel_launches() - launches0
+    clocks = clk.summary()
+    dev_mean, wall_mean = statistics.mean(dev_s), statistics.mean(wall_s)
+    if pg:
+        dev_mean, wall_mean = max_over_ranks(pg, [dev_mean, wall_mean], "cuda")
+    _lib.check(lib.pado_set_scratch_cache(0))
+    prof, roofline = {}, None
+    if not args.no_profile:
+        _lib.check(lib.pado_profile(1))
+        dev_once()
+        torch.cuda.synchronize()
+        prof = read_profile(lib)
+        _lib.check(lib.pado_profile(0))
+    peak, peak_src = peaks()
+    if prof:
+        tot_ms = sum(x["ms"] for x in prof.values())
+        top = max(prof, key=lambda k: prof[k]["ms"])
+        tk = prof[top]
+        per = ingest_kernel_bytes(top, m)
+        avg_s = tk["ms"] / 1e3 / max(tk["launches"], 1)
+        ach = per / avg_s / 1e9 if per else None
+        roofline = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": ach / peak if ach else None, "traffic": traffic_from_profiles(top, "ingest"),
+                    "peak_source": peak_src, "share_of_ingest_device_time": tk["ms"] / tot_ms if tot_ms else None,
+                    "launches": tk["launches"], "avg_launch_us": avg_s * 1e6, "bytes_per_launch": per}
+    cpu = None
+    if not args.no_cpu_baseline and grank == 0:
+        cv, sec, kind, cm = ingest_cpu(INGEST["ref_scale"])
+        cpu = {"value": cv, "unit": "edges/s", "cores": 1, "kind": kind, "seconds": sec,
+               "sample": f"raw R-MAT s{INGEST['ref_scale']} ef16 samples ({cm} edges), Graph(edge_list) + "
+                         f"degree order + id_transfer"}
+    if grank == 0:
+        h2d = 8 * m
+        d2h = 8 * (n + 1) + 4 * 2 * m + 4 * n
+        print(json.dumps({
+            "metric": "edges_per_s", "value": m * world / dev_mean, "unit": "edges/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_mean * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": "ingest", "desc": INGEST["desc"], "scale": args.ingest_scale, "edges": m, "n": n,
+                       "scratch_cache_bytes": INGEST["scratch_cache"],
+                       "entries": 2 * m, "l2": f"inputs larger than L2 ({8 * m / 1e6:.0f} MB of edges, "
+                                               f"{16 * m / 1e6:.0f} MB of sort keys)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": m * world / wall_mean, "unit": "edges/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "wall_s": wall_mean},
+            "compulsory_gbs": (8 * m + 4 * 2 * m + 8 * (n + 1) + 4 * n) / dev_mean / 1e9,
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
+            "profile": prof}), flush=True)
+    if pg:
+        pg.destroy_process_group()
 
 
 def attribute_loop_bytes(prof):

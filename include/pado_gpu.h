@@ -168,6 +168,14 @@ int pado_graph_ingest_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_
                              uint32_t flags, uint64_t *d_off, uint32_t *d_adj, uint8_t *d_w_out, uint32_t *d_rank,
                              uint64_t *entries, void *stream);
 
+/* The ingest calls take their scratch (sort keys and buffers, about 24
+ * bytes per edge) from a memory pool of the library's own, in stream order.
+ * Up to `bytes` of it stay reserved on the current device between calls
+ * (default 0: every call returns its scratch); a service that ingests
+ * graphs repeatedly keeps them to skip the device allocations.  Setting 0
+ * releases what is kept. */
+int pado_set_scratch_cache(uint64_t bytes);
+
 /* Ingest + labeling in one call, the graph staying on the device between
  * them: the index answers queries by ORIGINAL id (the reference's sequence
  * Graph -> make_rank -> id_transfer -> labeler -> order_labels, pado.cpp

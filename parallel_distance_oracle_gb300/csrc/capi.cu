@@ -250,24 +250,24 @@ void build_ingested(pado_index *h, pado::IngestResult &r, uint32_t K, uint32_t B
     pado::DevGraph g;
     g.n = n;
     g.m = r.m;
-    g.off.alloc((uint64_t)n + 1);
-    g.off.upload(r.off.data(), (uint64_t)n + 1, s);
+    g.off = std::move(r.off);
     g.adj = std::move(r.adj);
     g.w = std::move(r.w);
     // Root selection reads the lists of the first roots and their neighbours
     // only: root i is the smallest id no earlier root or selected neighbour
-    // took, so every root id is below 65 * K.  Only that prefix of the
-    // adjacency comes to the host.
+    // took, so every root id is below 65 * K.  The offsets and only that
+    // prefix of the adjacency come to the host.
     pado::HostGraph hg;
     hg.n = n;
-    hg.off = std::move(r.off);
+    hg.off.resize((uint64_t)n + 1);
+    g.off.download(hg.off.data(), (uint64_t)n + 1, s);
+    PADO_CUDA(cudaStreamSynchronize(s));
     if (h->kind == PADO_UNWEIGHTED && h->K) {
         const uint32_t R = (uint32_t)std::min<uint64_t>(n, 65ull * h->K);
         hg.adj.resize(hg.off[R]);
         g.adj.download(hg.adj.data(), hg.off[R], s);
     }
-    h->rank.alloc(std::max<uint32_t>(n, 1));
-    h->rank.upload(r.rank.data(), n, s);
+    h->rank = std::move(r.rank);
     PADO_CUDA(cudaStreamSynchronize(s));
     phase("upload");
     label_into(h, hg, g, h->K, B, s, phase);
@@ -555,6 +555,20 @@ int pado_w_build_ranked(uint32_t n, const uint64_t *off, const uint32_t *adj, co
     return build_common(true, n, off, adj, w, nullptr, 0, batch, out);
 }
 
+namespace {
+// Bytes of ingest scratch kept reserved between calls (pado_set_scratch_cache).
+std::atomic<uint64_t> g_scratch_keep{0};
+uint64_t scratch_keep() { return g_scratch_keep.load(std::memory_order_relaxed); }
+}  // namespace
+
+int pado_set_scratch_cache(uint64_t bytes)
+{
+    return guarded([&] {
+        g_scratch_keep.store(bytes, std::memory_order_relaxed);
+        pado::release_scratch(bytes);
+    });
+}
+
 int pado_graph_ingest(uint64_t m, const uint32_t *u, const uint32_t *v, const uint8_t *w, uint32_t n, uint32_t flags,
                       uint64_t *off, uint32_t *adj, uint8_t *w_out, uint32_t *rank, uint64_t *entries)
 {
@@ -572,11 +586,14 @@ int pado_graph_ingest(uint64_t m, const uint32_t *u, const uint32_t *v, const ui
         dv.upload(v, m, s);
         if (w) dw.upload(w, m, s);
         pado::IngestResult r = pado::ingest_edges(m, du.p, dv.p, w ? dw.p : nullptr, n, flags & PADO_INGEST_DEDUPE, s);
+        pado::DBuf<uint64_t> off64((uint64_t)n + 1);
+        pado::widen_u32(r.off.p, (uint64_t)n + 1, off64.p, s);
         r.adj.download(adj, r.m, s);
         if (w) r.w.download(w_out, r.m, s);
-        for (uint64_t k = 0; k <= n; ++k) off[k] = r.off[k];
-        std::memcpy(rank, r.rank.data(), (uint64_t)n * sizeof(uint32_t));
+        off64.download(off, (uint64_t)n + 1, s);
+        r.rank.download(rank, n, s);
         PADO_CUDA(cudaStreamSynchronize(s));
+        pado::release_scratch(scratch_keep());
         *entries = r.m;
     });
 }
@@ -593,10 +610,10 @@ int pado_graph_ingest_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_
         PADO_CHECK(!d_w || d_w_out || m == 0, PADO_E_ARG, "null weight output");
         const cudaStream_t s = (cudaStream_t)stream;
         pado::IngestResult r = pado::ingest_edges(m, d_u, d_v, d_w, n, flags & PADO_INGEST_DEDUPE, s, d_adj, d_w_out);
-        std::vector<uint64_t> off64(r.off.begin(), r.off.end());
-        PADO_CUDA(cudaMemcpyAsync(d_off, off64.data(), off64.size() * 8, cudaMemcpyHostToDevice, s));
-        PADO_CUDA(cudaMemcpyAsync(d_rank, r.rank.data(), (uint64_t)n * 4, cudaMemcpyHostToDevice, s));
+        pado::widen_u32(r.off.p, (uint64_t)n + 1, d_off, s);
+        if (n) PADO_CUDA(cudaMemcpyAsync(d_rank, r.rank.p, (uint64_t)n * 4, cudaMemcpyDeviceToDevice, s));
         PADO_CUDA(cudaStreamSynchronize(s));
+        pado::release_scratch(scratch_keep());
         *entries = r.m;
     });
 }
@@ -624,6 +641,7 @@ int edges_build(bool weighted, uint64_t m, const uint32_t *u, const uint32_t *v,
             if (weighted) dw.upload(w, m, s);
             r = pado::ingest_edges(m, du.p, dv.p, weighted ? dw.p : nullptr, n, flags & PADO_INGEST_DEDUPE, s);
         }
+        pado::release_scratch(scratch_keep());
         phase("ingest");
         build_ingested(h.get(), r, h->K, B, s, phase);
         *out = h.release();
@@ -662,6 +680,7 @@ int pado_build_edge_file(const char *path, uint32_t kind, uint32_t flags, uint32
             phase("read+parse");
             r = pado::ingest_edges(p.m, p.u.p, p.v.p, weighted ? p.w.p : nullptr, 0, flags & PADO_INGEST_DEDUPE, s);
         }
+        pado::release_scratch(scratch_keep());
         phase("ingest");
         build_ingested(h.get(), r, h->K, batch, s, phase);
         *out = h.release();

@@ -19,22 +19,30 @@
 //
 // Device mapping.  Text: newlines are located per 16-byte chunk (count, scan,
 // write), every line is parsed by one thread, and the parsed edges are
-// compacted in line order.  Graph: degrees are counted with atomics; the rank
-// order is a counting sort of the n degrees on the host (O(n + max degree));
-// each directed entry becomes one 64-bit key
+// compacted in line order.  Graph: degrees are counted in per-block shared
+// tables with a global fallback; the vertex order is a stable radix sort of (max degree - degree,
+// id) keys, so ties keep ascending ids; offsets are the scan of the degrees in
+// rank order.  Each directed entry becomes one 64-bit key
 //     rank(src) << (b + 8) | (2^b - 1 - rank(dst)) << 8 | (255 - weight)
 // (b = bits of n), so ascending key order is "by source rank, then
 // destination rank descending, then weight descending"; the keys are sorted
-// by a stable LSD radix sort (8-bit digits, a warp per tile: per-tile digit
-// counts, one exclusive scan over (digit, tile), then a scatter in which
-// lanes holding the same digit are ranked with __match_any_sync), and the
-// adjacency and weights are read back out of the sorted keys.  Offsets follow
-// from the degrees in rank order.
+// by the same stable LSD radix sort and the adjacency and weights are read
+// back out of them.
+//
+// The radix sort: 8-bit digits, tiles of 4096 keys, three kernels per digit
+// -- per-tile digit counts, one exclusive scan over the (digit, tile) matrix,
+// and a scatter in which each block ranks its tile's keys by digit (lanes
+// holding the same digit ranked with __match_any_sync, warps by a prefix over
+// the block), reorders the tile in shared memory and writes every digit's
+// run to its global position in coalesced stores.
 
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <optional>
 
 #include "pado_internal.cuh"
 
@@ -42,9 +50,10 @@ namespace pado {
 namespace {
 
 constexpr unsigned FULLW = 0xffffffffu;
-constexpr uint32_t RS_TILE = 2048;   // keys per warp tile in the radix sort
-constexpr int RS_WARPS = 8;          // warps per block
-constexpr uint32_t TEXT_CHUNK = 16;  // bytes per thread when locating newlines
+constexpr int RS_THREADS = 256;                  // radix sort block
+constexpr int RS_PER = 16;                       // keys per thread
+constexpr uint32_t RS_TILE = RS_THREADS * RS_PER;  // 4096 keys per tile
+constexpr uint32_t TEXT_CHUNK = 16;              // bytes per thread when locating newlines
 
 // ---- scan -------------------------------------------------------------------
 
@@ -97,15 +106,24 @@ __global__ void __launch_bounds__(1024) scan_add_kernel(uint32_t *a, uint64_t L,
     if (i < L) a[i] += sums[blockIdx.x];
 }
 
-// In place; the caller keeps the sums below 2^32.
-void exclusive_scan(uint32_t *a, uint64_t L, cudaStream_t s)
+uint64_t scan_sums_needed(uint64_t L) { return std::max<uint64_t>((L + 1023) / 1024, 1); }
+
+// In place, stream-ordered; `sums` holds scan_sums_needed(L) entries; the
+// caller keeps the total below 2^32.
+void exclusive_scan(uint32_t *a, uint64_t L, uint32_t *sums, cudaStream_t s)
 {
     if (L == 0) return;
     const uint32_t nb = (uint32_t)((L + 1023) / 1024);
-    DBuf<uint32_t> sums(nb);
-    PADO_LAUNCH("scan_block_kernel", s, scan_block_kernel<<<nb, 1024, 0, s>>>(a, L, sums.p));
-    PADO_LAUNCH("scan_sums_kernel", s, scan_sums_kernel<<<1, 1024, 0, s>>>(sums.p, nb));
-    PADO_LAUNCH("scan_add_kernel", s, scan_add_kernel<<<nb, 1024, 0, s>>>(a, L, sums.p));
+    PADO_LAUNCH("scan_block_kernel", s, scan_block_kernel<<<nb, 1024, 0, s>>>(a, L, sums));
+    PADO_LAUNCH("scan_sums_kernel", s, scan_sums_kernel<<<1, 1024, 0, s>>>(sums, nb));
+    PADO_LAUNCH("scan_add_kernel", s, scan_add_kernel<<<nb, 1024, 0, s>>>(a, L, sums));
+}
+
+// Same with its own block-sum buffer; completes before returning.
+void exclusive_scan(uint32_t *a, uint64_t L, cudaStream_t s)
+{
+    DBuf<uint32_t> sums(scan_sums_needed(L));
+    exclusive_scan(a, L, sums.p, s);
     PADO_CUDA(cudaStreamSynchronize(s));  // `sums` is freed on return
 }
 
@@ -118,73 +136,194 @@ T read_back(const T *d, cudaStream_t s)
     return x;
 }
 
+// Scratch comes from a memory pool of this library's own (one per device),
+// allocated and freed in stream order: a call's buffers are reused by its
+// later steps without device-wide synchronisation, and up to
+// the caller's chosen amount stays reserved for the next call
+// (release_scratch trims it).
+cudaMemPool_t scratch_pool()
+{
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    int dev = 0;
+    PADO_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = pools.find(dev);
+    if (it != pools.end()) return it->second;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    PADO_CUDA(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep = ~0ull;  // nothing is returned implicitly at synchronisation points
+    PADO_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    pools[dev] = pool;
+    return pool;
+}
+
+template <typename T>
+struct PBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = nullptr;
+    PBuf(size_t count, cudaStream_t st) : n(count), s(st)
+    {
+        if (count) PADO_CUDA(cudaMallocFromPoolAsync((void **)&p, count * sizeof(T), scratch_pool(), s));
+    }
+    PBuf(const PBuf &) = delete;
+    PBuf &operator=(const PBuf &) = delete;
+    ~PBuf()
+    {
+        if (p) cudaFreeAsync(p, s);
+    }
+    void zero()
+    {
+        if (n) PADO_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+};
+
 // ---- radix sort -------------------------------------------------------------
 
 // counts[d * ntiles + tile] = keys of `tile` whose digit at `shift` is d.
-__global__ void __launch_bounds__(RS_WARPS * 32) rs_hist_kernel(const uint64_t *keys, uint64_t L, uint32_t shift,
-                                                                uint32_t ntiles, uint32_t *counts)
+__global__ void __launch_bounds__(RS_THREADS) rs_hist_kernel(const uint64_t *keys, uint64_t L, uint32_t shift,
+                                                             uint32_t ntiles, uint32_t *counts)
 {
-    __shared__ uint32_t h[RS_WARPS][256];
-    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < ntiles; tile += nw) {
-        for (int d = lane; d < 256; d += 32) h[wl][d] = 0;
-        __syncwarp();
+    __shared__ uint32_t h[256];
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        h[threadIdx.x] = 0;
+        __syncthreads();
         const uint64_t t0 = (uint64_t)tile * RS_TILE, t1 = min(L, t0 + RS_TILE);
-        for (uint64_t i = t0 + lane; i < t1; i += 32) atomicAdd(&h[wl][(keys[i] >> shift) & 255u], 1u);
-        __syncwarp();
-        for (int d = lane; d < 256; d += 32) counts[(uint64_t)d * ntiles + tile] = h[wl][d];
-        __syncwarp();
+        for (uint64_t i = t0 + threadIdx.x; i < t1; i += RS_THREADS)
+            atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+        __syncthreads();
+        counts[(uint64_t)threadIdx.x * ntiles + tile] = h[threadIdx.x];
+        __syncthreads();
     }
 }
 
-// Stable scatter: a tile's keys in order, 32 at a time; lanes holding the
-// same digit are ranked by lane order.
-__global__ void __launch_bounds__(RS_WARPS * 32) rs_scatter_kernel(const uint64_t *in, uint64_t *out, uint64_t L,
-                                                                   uint32_t shift, uint32_t ntiles,
-                                                                   const uint32_t *offsets)
+// Stable scatter of one digit.  Warp w owns keys [512 w, 512 w + 512) of the
+// tile, 32 per round; a key's place among the tile's keys with its digit is
+// (keys of lower warps) + (keys of earlier rounds of its warp) + (lower lanes
+// of its round), which is its input order.  A thread's 16 keys are loaded
+// before any ranking so that their loads are in flight together.
+__global__ void __launch_bounds__(RS_THREADS, 4) rs_scatter_kernel(const uint64_t *in, uint64_t *out, uint64_t L,
+                                                                uint32_t shift, uint32_t ntiles,
+                                                                const uint32_t *offsets)
 {
-    __shared__ uint32_t base[RS_WARPS][256];
+    constexpr int NW = RS_THREADS / 32;
+    __shared__ uint64_t sk[RS_TILE];      // the tile, reordered by digit
+    __shared__ uint16_t slr[RS_TILE];     // rank of key i among its warp's keys with its digit
+    __shared__ uint16_t wcnt[NW][256];    // per warp and digit: count, then prefix over warps
+    __shared__ uint32_t dstart[256];      // first slot of each digit in the reordered tile
+    __shared__ uint32_t gbase[256];       // global position of each digit's run
+    __shared__ uint32_t wsum[NW];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t below = (1u << lane) - 1u;
-    for (uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < ntiles; tile += nw) {
-        for (int d = lane; d < 256; d += 32) base[wl][d] = offsets[(uint64_t)d * ntiles + tile];
-        __syncwarp();
-        const uint64_t t0 = (uint64_t)tile * RS_TILE, t1 = min(L, t0 + RS_TILE);
-        for (uint64_t c0 = t0; c0 < t1; c0 += 32) {
-            const uint64_t i = c0 + lane;
-            const bool live = i < t1;
-            const uint64_t key = live ? in[i] : 0ull;
-            const uint32_t dig = live ? (uint32_t)((key >> shift) & 255u) : 256u + lane;  // idle lanes stand alone
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t t0 = (uint64_t)tile * RS_TILE;
+        const uint32_t cnt = (uint32_t)min(L - t0, (uint64_t)RS_TILE);
+        const uint32_t i0 = wl * (RS_PER * 32) + lane;
+        uint64_t key[RS_PER];
+#pragma unroll
+        for (int r = 0; r < RS_PER; ++r) key[r] = i0 + r * 32 < cnt ? in[t0 + i0 + r * 32] : 0ull;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) wcnt[w][threadIdx.x] = 0;
+        gbase[threadIdx.x] = offsets[(uint64_t)threadIdx.x * ntiles + tile];
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < RS_PER; ++r) {
+            const uint32_t i = i0 + r * 32;
+            const bool live = i < cnt;
+            const uint32_t dig = live ? (uint32_t)((key[r] >> shift) & 255u) : 256u + lane;  // idle lanes alone
             const uint32_t peers = __match_any_sync(FULLW, dig);
-            if (live) out[base[wl][dig] + __popc(peers & below)] = key;
+            if (live) slr[i] = (uint16_t)(wcnt[wl][dig] + __popc(peers & below));
             __syncwarp();
-            if (live && (peers & below) == 0) base[wl][dig] += __popc(peers);
+            if (live && (peers & below) == 0) wcnt[wl][dig] += (uint16_t)__popc(peers);
             __syncwarp();
         }
+        __syncthreads();
+        // thread d: prefix of digit d over the warps, and the digit's total
+        uint32_t tot = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            const uint32_t c = wcnt[w][threadIdx.x];
+            wcnt[w][threadIdx.x] = (uint16_t)tot;
+            tot += c;
+        }
+        // exclusive scan of the 256 totals -> dstart
+        uint32_t inc = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULLW, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wsum[wl] = inc;
+        __syncthreads();
+        uint32_t wpre = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) wpre += w < wl ? wsum[w] : 0u;
+        dstart[threadIdx.x] = wpre + inc - tot;
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < RS_PER; ++r) {
+            const uint32_t i = i0 + r * 32;
+            if (i < cnt) {
+                const uint32_t dig = (uint32_t)((key[r] >> shift) & 255u);
+                sk[dstart[dig] + wcnt[wl][dig] + slr[i]] = key[r];
+            }
+        }
+        __syncthreads();
+        for (uint32_t p = threadIdx.x; p < cnt; p += RS_THREADS) {
+            const uint64_t k = sk[p];
+            const uint32_t dig = (uint32_t)((k >> shift) & 255u);
+            out[gbase[dig] + (p - dstart[dig])] = k;
+        }
+        __syncthreads();
     }
 }
 
-// Sorts keys[0, L) ascending on bits [lo, hi), stably; the result is in `keys`.
-void radix_sort(DBuf<uint64_t> &keys, uint64_t L, uint32_t lo, uint32_t hi, cudaStream_t s)
+uint64_t sort_tiles(uint64_t L) { return std::max<uint64_t>((L + RS_TILE - 1) / RS_TILE, 1); }
+
+// Scratch of a radix sort of up to L keys.
+struct SortSpace {
+    PBuf<uint64_t> tmp;
+    PBuf<uint32_t> counts, sums;
+    SortSpace(uint64_t L, cudaStream_t s)
+        : tmp(std::max<uint64_t>(L, 1), s), counts(256 * sort_tiles(L), s),
+          sums(scan_sums_needed(256 * sort_tiles(L)), s)
+    {
+    }
+};
+
+// Sorts keys[0, L) ascending on bits [lo, hi), stably, stream-ordered;
+// returns the buffer holding the result (`keys` or ws.tmp).  The dedupe and
+// vertex-order sorts (`aux`) are profiled under their own names, so that the
+// entry sort's launches all process the same 2m keys.
+uint64_t *radix_sort(uint64_t *keys, uint64_t L, uint32_t lo, uint32_t hi, SortSpace &ws, cudaStream_t s,
+                     bool aux = false)
 {
-    if (L < 2 || lo >= hi) return;
+    if (L < 2 || lo >= hi) return keys;
+    PADO_CHECK(ws.tmp.n >= L, PADO_E_ARG, "sort scratch too small");
     const uint32_t ntiles = (uint32_t)((L + RS_TILE - 1) / RS_TILE);
-    DBuf<uint64_t> tmp(L);
-    DBuf<uint32_t> counts((uint64_t)256 * ntiles);
-    const unsigned grid = grid_for((uint64_t)ntiles * 32, RS_WARPS * 32, 152u * 16u);
-    uint64_t *src = keys.p, *dst = tmp.p;
+    const unsigned grid = std::min<uint32_t>(ntiles, 152u * 8u);
+    const char *hname = aux ? "rs_hist_kernel.aux" : "rs_hist_kernel";
+    const char *sname = aux ? "rs_scatter_kernel.aux" : "rs_scatter_kernel";
+    uint64_t *src = keys, *dst = ws.tmp.p;
     for (uint32_t shift = lo; shift < hi; shift += 8) {
-        PADO_LAUNCH("rs_hist_kernel", s,
-                    rs_hist_kernel<<<grid, RS_WARPS * 32, 0, s>>>(src, L, shift, ntiles, counts.p));
-        exclusive_scan(counts.p, (uint64_t)256 * ntiles, s);
-        PADO_LAUNCH("rs_scatter_kernel", s,
-                    rs_scatter_kernel<<<grid, RS_WARPS * 32, 0, s>>>(src, dst, L, shift, ntiles, counts.p));
+        PADO_LAUNCH(hname, s, rs_hist_kernel<<<grid, RS_THREADS, 0, s>>>(src, L, shift, ntiles, ws.counts.p));
+        exclusive_scan(ws.counts.p, (uint64_t)256 * ntiles, ws.sums.p, s);
+        PADO_LAUNCH(sname, s, rs_scatter_kernel<<<grid, RS_THREADS, 0, s>>>(src, dst, L, shift, ntiles, ws.counts.p));
         std::swap(src, dst);
     }
-    if (src != keys.p) PADO_CUDA(cudaMemcpyAsync(keys.p, src, L * 8, cudaMemcpyDeviceToDevice, s));
-    PADO_CUDA(cudaStreamSynchronize(s));  // `tmp` and `counts` are freed on return
+    return src;
+}
+
+uint32_t id_bits(uint64_t n)
+{
+    uint32_t b = 1;
+    while (b < 40 && (1ull << b) < n) ++b;
+    return b;
 }
 
 // ---- edge list -> ranked CSR ------------------------------------------------
@@ -245,17 +384,76 @@ __global__ void __launch_bounds__(256) unique_scatter_kernel(const uint64_t *key
     }
 }
 
+// deg[x] += 1 for both ends of every edge.  Each block counts its share of
+// the edges in a shared-memory table of DEG_SLOTS (vertex, count) slots,
+// claimed by the first vertex that hashes there; vertices that find their
+// slot taken add to global memory directly.  The heavy vertices of a skewed
+// graph claim their slots early (they are most of the endpoints) and then
+// cost one global atomic per block instead of one per endpoint.
+constexpr uint32_t DEG_SLOTS = 2048;
+
+__device__ __forceinline__ void count_endpoint(uint32_t a, uint32_t *cid, uint32_t *ccnt, uint32_t *deg)
+{
+    const uint32_t slot = (a * 2654435761u) >> 21;  // top 11 bits: DEG_SLOTS slots
+    const uint32_t old = atomicCAS(&cid[slot], 0xffffffffu, a);
+    if (old == 0xffffffffu || old == a)
+        atomicAdd(&ccnt[slot], 1u);
+    else
+        atomicAdd(&deg[a], 1u);
+}
+
 __global__ void __launch_bounds__(256) degree_kernel(const uint32_t *u, const uint32_t *v, uint64_t m, uint32_t n,
                                                      uint32_t *deg, uint32_t *bad)
 {
+    __shared__ uint32_t cid[DEG_SLOTS], ccnt[DEG_SLOTS];
+    for (uint32_t k = threadIdx.x; k < DEG_SLOTS; k += blockDim.x) {
+        cid[k] = 0xffffffffu;
+        ccnt[k] = 0;
+    }
+    __syncthreads();
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t a = u[e], b = v[e];
         if (a >= n || b >= n) {
             atomicOr(bad, 1u);
             continue;
         }
-        atomicAdd(&deg[a], 1u);
-        atomicAdd(&deg[b], 1u);
+        count_endpoint(a, cid, ccnt, deg);
+        count_endpoint(b, cid, ccnt, deg);
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < DEG_SLOTS; k += blockDim.x)
+        if (ccnt[k]) atomicAdd(&deg[cid[k]], ccnt[k]);
+}
+
+__global__ void __launch_bounds__(256) max_deg_kernel(const uint32_t *deg, uint32_t n, uint32_t *mx)
+{
+    uint32_t x = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x = max(x, deg[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(FULLW, x, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, x);
+}
+
+// (max degree - degree, id): ascending order = degree descending, ties by id.
+__global__ void __launch_bounds__(256) order_key_kernel(const uint32_t *deg, uint32_t n, uint32_t maxdeg,
+                                                        uint64_t *keys)
+{
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x)
+        keys[x] = (uint64_t)(maxdeg - deg[x]) << 32 | x;
+}
+
+// rank[id] = position; degr[position] = degree (degr[n] = 0 closes the scan).
+__global__ void __launch_bounds__(256) rank_kernel(const uint64_t *keys, uint32_t n, uint32_t maxdeg, uint32_t *rank,
+                                                   uint32_t *degr)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p <= n; p += gridDim.x * blockDim.x) {
+        if (p == n) {
+            degr[n] = 0;
+            continue;
+        }
+        const uint64_t k = keys[p];
+        rank[(uint32_t)k] = p;
+        degr[p] = maxdeg - (uint32_t)(k >> 32);
     }
 }
 
@@ -284,11 +482,10 @@ __global__ void __launch_bounds__(256) extract_kernel(const uint64_t *keys, uint
     }
 }
 
-uint32_t id_bits(uint32_t n)
+__global__ void __launch_bounds__(256) widen_kernel(const uint32_t *a, uint64_t n, uint64_t *b)
 {
-    uint32_t b = 1;
-    while (b < 32 && (1ull << b) < n) ++b;
-    return b;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        b[i] = a[i];
 }
 
 // ---- text -------------------------------------------------------------------
@@ -390,9 +587,9 @@ IngestResult ingest_edges(uint64_t m, const uint32_t *du, const uint32_t *dv, co
 {
     IngestResult r;
     PADO_CHECK(m < (1ull << 31), PADO_E_ARG, "at most 2^31 - 1 edges (2^32 - 2 adjacency entries)");
-    DBuf<uint32_t> scal(1);
+    PBuf<uint32_t> scal(1, s);
     if (n == 0 && m) {  // n = max id + 1, as Graph::construct sets it
-        scal.fill_bytes(0, s);
+        scal.zero();
         PADO_LAUNCH("max_id_kernel", s, max_id_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, m, scal.p));
         const uint32_t mx = read_back(scal.p, s);
         PADO_CHECK(mx < 0xffffffffu, PADO_E_ARG, "vertex id 2^32 - 1 is reserved");
@@ -401,53 +598,62 @@ IngestResult ingest_edges(uint64_t m, const uint32_t *du, const uint32_t *dv, co
     const uint32_t bits = id_bits(n);
     PADO_CHECK(bits <= 28, PADO_E_ARG, "graph ingest supports fewer than 2^28 vertices");
     r.n = n;
+    // one sort scratch for every sort of the call: the dedupe sort (m keys),
+    // the order sort (n keys) and the entry sort (2m keys after dedupe)
+    SortSpace ws(std::max<uint64_t>(2 * m, n), s);
 
     // optional dedupe over original ids
-    DBuf<uint32_t> u2, v2;
-    DBuf<uint8_t> w2;
+    std::optional<PBuf<uint32_t>> u2, v2;
+    std::optional<PBuf<uint8_t>> w2;
     if (dedupe && m) {
-        DBuf<uint64_t> ck(m);
-        scal.fill_bytes(0, s);
+        PBuf<uint64_t> ck(m, s);
+        scal.zero();
         PADO_LAUNCH("canon_key_kernel", s,
                     canon_key_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, dw, m, n, bits, ck.p, scal.p));
         PADO_CHECK(read_back(scal.p, s) == 0, PADO_E_ARG, "edge endpoint out of range");
-        radix_sort(ck, m, 8, 2 * bits + 8, s);
-        DBuf<uint32_t> pos(m + 1);
-        PADO_LAUNCH("unique_flag_kernel", s, unique_flag_kernel<<<grid_for(m + 1, 256), 256, 0, s>>>(ck.p, m, pos.p));
-        exclusive_scan(pos.p, m + 1, s);
+        const uint64_t *sorted = radix_sort(ck.p, m, 8, 2 * bits + 8, ws, s, true);
+        PBuf<uint32_t> pos(m + 1, s), psums(scan_sums_needed(m + 1), s);
+        PADO_LAUNCH("unique_flag_kernel", s,
+                    unique_flag_kernel<<<grid_for(m + 1, 256), 256, 0, s>>>(sorted, m, pos.p));
+        exclusive_scan(pos.p, m + 1, psums.p, s);
         const uint32_t mu = read_back(pos.p + m, s);
-        u2.alloc(std::max<uint32_t>(mu, 1));
-        v2.alloc(std::max<uint32_t>(mu, 1));
-        if (dw) w2.alloc(std::max<uint32_t>(mu, 1));
+        u2.emplace(std::max<uint32_t>(mu, 1), s);
+        v2.emplace(std::max<uint32_t>(mu, 1), s);
+        if (dw) w2.emplace(std::max<uint32_t>(mu, 1), s);
         PADO_LAUNCH("unique_scatter_kernel", s,
-                    unique_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(ck.p, m, bits, pos.p, u2.p, v2.p,
-                                                                         dw ? w2.p : nullptr));
-        PADO_CUDA(cudaStreamSynchronize(s));
-        du = u2.p;
-        dv = v2.p;
-        dw = dw ? w2.p : nullptr;
+                    unique_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(sorted, m, bits, pos.p, u2->p, v2->p,
+                                                                         dw ? w2->p : nullptr));
+        du = u2->p;
+        dv = v2->p;
+        dw = dw ? w2->p : nullptr;
         m = mu;
     }
 
-    // degrees -> rank (degree descending, ties by ascending id) -> offsets
-    DBuf<uint32_t> deg(std::max<uint32_t>(n, 1));
-    deg.fill_bytes(0, s);
-    scal.fill_bytes(0, s);
-    if (m)
-        PADO_LAUNCH("degree_kernel", s, degree_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, m, n, deg.p, scal.p));
-    std::vector<uint32_t> hdeg(n);
-    deg.download(hdeg.data(), n, s);
-    PADO_CHECK(read_back(scal.p, s) == 0, PADO_E_ARG, "edge endpoint out of range");
-    uint32_t maxdeg = 0;
-    for (uint32_t x = 0; x < n; ++x) maxdeg = std::max(maxdeg, hdeg[x]);
-    std::vector<uint32_t> start((uint64_t)maxdeg + 2, 0);
-    for (uint32_t x = 0; x < n; ++x) ++start[maxdeg - hdeg[x] + 1];
-    for (uint64_t k = 1; k < start.size(); ++k) start[k] += start[k - 1];
-    r.rank.resize(n);
-    for (uint32_t x = 0; x < n; ++x) r.rank[x] = start[maxdeg - hdeg[x]]++;
-    r.off.assign((uint64_t)n + 1, 0);
-    for (uint32_t x = 0; x < n; ++x) r.off[r.rank[x] + 1] = hdeg[x];
-    for (uint32_t k = 0; k < n; ++k) r.off[k + 1] += r.off[k];
+    // degrees -> order (degree descending, ties by ascending id) -> offsets
+    r.rank.alloc(std::max<uint32_t>(n, 1));
+    r.off.alloc((uint64_t)n + 1);
+    {
+        PBuf<uint32_t> deg(std::max<uint32_t>(n, 1), s);
+        deg.zero();
+        scal.zero();
+        if (m)
+            PADO_LAUNCH("degree_kernel", s,
+                        degree_kernel<<<grid_for(m, 256, 152u * 8u), 256, 0, s>>>(du, dv, m, n, deg.p, scal.p));
+        PADO_CHECK(read_back(scal.p, s) == 0, PADO_E_ARG, "edge endpoint out of range");
+        scal.zero();
+        if (n) PADO_LAUNCH("max_deg_kernel", s, max_deg_kernel<<<grid_for(n, 256), 256, 0, s>>>(deg.p, n, scal.p));
+        const uint32_t maxdeg = read_back(scal.p, s);
+        PBuf<uint64_t> ok(std::max<uint32_t>(n, 1), s);
+        if (n)
+            PADO_LAUNCH("order_key_kernel", s,
+                        order_key_kernel<<<grid_for(n, 256), 256, 0, s>>>(deg.p, n, maxdeg, ok.p));
+        const uint64_t *order =
+            radix_sort(ok.p, n, 32, 32 + (maxdeg ? id_bits((uint64_t)maxdeg + 1) : 0), ws, s, true);
+        PADO_LAUNCH("rank_kernel", s,
+                    rank_kernel<<<grid_for((uint64_t)n + 1, 256), 256, 0, s>>>(order, n, maxdeg, r.rank.p, r.off.p));
+        PBuf<uint32_t> osums(scan_sums_needed((uint64_t)n + 1), s);
+        exclusive_scan(r.off.p, (uint64_t)n + 1, osums.p, s);
+    }
 
     // keys -> sort -> adjacency (and weights)
     const uint64_t L = 2 * m;
@@ -461,18 +667,26 @@ IngestResult ingest_edges(uint64_t m, const uint32_t *du, const uint32_t *dv, co
         w_out = r.w.p;
     }
     if (L) {
-        DBuf<uint32_t> drank(n);
-        drank.upload(r.rank.data(), n, s);
-        DBuf<uint64_t> keys(L);
+        PBuf<uint64_t> keys(L, s);
         PADO_LAUNCH("entry_key_kernel", s,
-                    entry_key_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, dw, m, drank.p, bits, keys.p));
+                    entry_key_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, dw, m, r.rank.p, bits, keys.p));
         // after dedupe no (src, dst) pair repeats, so the weight byte needs no pass
-        radix_sort(keys, L, dw && !dedupe ? 0u : 8u, 2 * bits + 8, s);
+        const uint64_t *sorted = radix_sort(keys.p, L, dw && !dedupe ? 0u : 8u, 2 * bits + 8, ws, s);
         PADO_LAUNCH("extract_kernel", s,
-                    extract_kernel<<<grid_for(L, 256), 256, 0, s>>>(keys.p, L, bits, adj_out, dw ? w_out : nullptr));
-        PADO_CUDA(cudaStreamSynchronize(s));
+                    extract_kernel<<<grid_for(L, 256), 256, 0, s>>>(sorted, L, bits, adj_out, dw ? w_out : nullptr));
     }
+    PADO_CUDA(cudaStreamSynchronize(s));
     return r;
+}
+
+void release_scratch(uint64_t keep_bytes)
+{
+    PADO_CUDA(cudaMemPoolTrimTo(scratch_pool(), keep_bytes));
+}
+
+void widen_u32(const uint32_t *a, uint64_t n, uint64_t *b, cudaStream_t s)
+{
+    if (n) PADO_LAUNCH("widen_kernel", s, widen_kernel<<<grid_for(n, 256), 256, 0, s>>>(a, n, b));
 }
 
 // ---- text parsing -----------------------------------------------------------
@@ -578,3 +792,4 @@ EdgeTextParser read_edge_file(const char *path, bool weighted, cudaStream_t s)
 }
 
 }  // namespace pado
+

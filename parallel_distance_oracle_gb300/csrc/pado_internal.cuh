@@ -114,16 +114,20 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
 // drops self-loops and merges repeated pairs (first weight wins) first.  The
 // adjacency (and weights) go to adj_out / w_out (device, room for 2m) when
 // given, else into the result's own buffers.
-struct IngestResult {
+struct IngestResult {  // all on the device
     uint32_t n = 0;
     uint64_t m = 0;                  // directed entries
-    std::vector<uint32_t> rank;      // original id -> rank
-    std::vector<uint32_t> off;       // n + 1, rank-indexed
+    DBuf<uint32_t> rank;             // n: original id -> rank
+    DBuf<uint32_t> off;              // n + 1, rank-indexed
     DBuf<uint32_t> adj;              // m: rank ids, every list descending (id, weight)
     DBuf<uint8_t> w;                 // m (weighted only)
 };
 IngestResult ingest_edges(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, const uint8_t *d_w, uint32_t n,
                           bool dedupe, cudaStream_t s, uint32_t *adj_out = nullptr, uint8_t *w_out = nullptr);
+// Trims the ingest scratch pool of the current device to keep_bytes.
+void release_scratch(uint64_t keep_bytes);
+// b[i] = a[i] for i < n (device arrays, stream-ordered).
+void widen_u32(const uint32_t *a, uint64_t n, uint64_t *b, cudaStream_t s);
 
 // Edge-list text ("head tail [weight]" lines, graph.h:95-117, :262-290)
 // parsed on the device into u / v / w (device, m edges so far, in line

@@ -206,3 +206,46 @@ def test_build_edge_file_missing_is_io_error(pado, tmp_path):
     from parallel_distance_oracle_gb300 import _lib
     with pytest.raises(_lib.PadoError, match="cannot open"):
         pado.VertexCentricPLL.from_edge_file(tmp_path / "absent.txt")
+
+
+def test_ingest_device_pointers_equal_host_call(pado):
+    """pado_graph_ingest_device on torch device tensors, on a caller stream."""
+    import ctypes as C
+
+    import torch
+    from parallel_distance_oracle_gb300 import _lib
+    n, u, v, w = G.rmat_edges(13, 8, 6, weights=(1, 100))
+    u, v = u.astype(np.uint32), v.astype(np.uint32)
+    m = len(u)
+    want, wrank = pado.graph_ingest(u, v, w, n=n)
+    du = torch.from_numpy(u.view(np.int32)).cuda()
+    dv = torch.from_numpy(v.view(np.int32)).cuda()
+    dw = torch.from_numpy(w).cuda()
+    off = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    adj = torch.zeros(2 * m, dtype=torch.int32, device="cuda")
+    wo = torch.zeros(2 * m, dtype=torch.uint8, device="cuda")
+    rank = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ent = C.c_uint64()
+    s = torch.cuda.Stream()
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    _lib.check(_lib.lib.pado_graph_ingest_device(m, P(du), P(dv), P(dw), n, 0, P(off), P(adj), P(wo), P(rank),
+                                                 C.byref(ent), C.c_void_p(s.cuda_stream)))
+    assert ent.value == len(want.adj)
+    assert np.array_equal(off.cpu().numpy().view(np.uint64), want.off)
+    assert np.array_equal(adj.cpu().numpy().view(np.uint32), want.adj)
+    assert np.array_equal(wo.cpu().numpy(), want.w)
+    assert np.array_equal(rank.cpu().numpy().view(np.uint32), wrank)
+
+
+def test_scratch_cache_keeps_results(pado):
+    """With scratch kept between calls, repeated ingests give the same CSR."""
+    from parallel_distance_oracle_gb300 import _lib
+    n, u, v, _ = G.rmat_edges(12, 8, 7)
+    want, wrank = orc.graph_ingest(u, v, n=n)
+    _lib.check(_lib.lib.pado_set_scratch_cache(1 << 30))
+    try:
+        for _ in range(3):
+            got, grank = pado.graph_ingest(u, v, n=n)
+            same(got, grank, want, wrank, "cached scratch")
+    finally:
+        _lib.check(_lib.lib.pado_set_scratch_cache(0))
