@@ -659,26 +659,11 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     if (lane == 0) wr.ctr[0] = 0;
     __syncwarp();
     // (b) gather first offers from active neighbours (heads >= s), 64
-    // neighbours per step so that two chunks' gathers are in flight at once
+    // neighbours per step.  The hubs of all active heads' last groups are
+    // flattened into one item list (inclusive counts sa / sb over the two
+    // halves) and spread over the lanes, so one round of loads covers 32 hubs
+    // whichever heads they belong to.
     const uint32_t e_end = d.off[t + 1];
-    auto offer_from = [&](uint32_t mask, uint64_t mpos, uint32_t mcnt) {
-        while (mask) {
-            const int src = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const uint64_t pos = __shfl_sync(FULL, mpos, src);
-            const uint32_t c = __shfl_sync(FULL, mcnt, src);
-            bytes += 12 + 4ull * c;  // last-group position/count and its hubs
-            for (uint32_t j = lane; j < c; j += 32) {
-                const uint32_t r = d.pool_hub[pos + j];
-                if (r < t) {
-                    const uint32_t idx = r - s;
-                    const uint32_t bit = 1u << (idx & 31);
-                    const uint32_t old = atomicOr(&wr.ind[idx >> 5], bit);
-                    if (!(old & bit)) wr.offered[atomicAdd(&wr.ctr[0], 1u)] = (uint16_t)idx;
-                }
-            }
-        }
-    };
     for (uint32_t e0 = d.off[t]; e0 < e_end; e0 += 64) {
         const uint32_t ea = e0 + lane, eb = ea + 32;
         const bool ina = ea < e_end, inb = eb < e_end;
@@ -689,10 +674,42 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         // every active head's last-group position and size, loaded in parallel
         const uint64_t pa = acta ? d.last_pos[pp][ha] : 0ull, pb = actb ? d.last_pos[pp][hb] : 0ull;
         const uint32_t ca = acta ? d.last_cnt[pp][ha] : 0u, cb = actb ? d.last_cnt[pp][hb] : 0u;
+        uint32_t sa = ca, sb = cb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t ya = __shfl_up_sync(FULL, sa, o), yb = __shfl_up_sync(FULL, sb, o);
+            if (lane >= o) {
+                sa += ya;
+                sb += yb;
+            }
+        }
+        const uint32_t ta = __shfl_sync(FULL, sa, 31), tot = ta + __shfl_sync(FULL, sb, 31);
         bytes += __popc(__ballot_sync(FULL, ina)) * 4ull + __popc(__ballot_sync(FULL, gea)) * 4ull +
-                 __popc(__ballot_sync(FULL, inb)) * 4ull + __popc(__ballot_sync(FULL, geb)) * 4ull;
-        offer_from(__ballot_sync(FULL, acta), pa, ca);
-        offer_from(__ballot_sync(FULL, actb), pb, cb);
+                 __popc(__ballot_sync(FULL, inb)) * 4ull + __popc(__ballot_sync(FULL, geb)) * 4ull +
+                 12ull * (__popc(__ballot_sync(FULL, acta)) + __popc(__ballot_sync(FULL, actb))) + 4ull * tot;
+        for (uint32_t i0 = 0; i0 < tot; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool second = i >= ta;
+            const uint32_t key = second ? i - ta : i;
+            // head lane: the number of lanes of the half whose inclusive count is <= key
+            uint32_t L = 0;
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1) {
+                const uint32_t va = __shfl_sync(FULL, sa, L + step - 1), vb = __shfl_sync(FULL, sb, L + step - 1);
+                if ((second ? vb : va) <= key) L += step;
+            }
+            const uint64_t qa = __shfl_sync(FULL, pa, L), qb = __shfl_sync(FULL, pb, L);
+            const uint32_t xa = __shfl_sync(FULL, sa - ca, L), xb = __shfl_sync(FULL, sb - cb, L);
+            if (i < tot) {
+                const uint32_t r = d.pool_hub[(second ? qb : qa) + (key - (second ? xb : xa))];
+                if (r < t) {
+                    const uint32_t idx = r - s;
+                    const uint32_t bit = 1u << (idx & 31);
+                    const uint32_t old = atomicOr(&wr.ind[idx >> 5], bit);
+                    if (!(old & bit)) wr.offered[atomicAdd(&wr.ctr[0], 1u)] = (uint16_t)idx;
+                }
+            }
+        }
         // descending list: once a neighbour is < s, the rest are too
         if (__ballot_sync(FULL, (ina && !gea) || (inb && !geb))) break;
     }
