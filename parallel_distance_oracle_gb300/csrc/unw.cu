@@ -151,10 +151,8 @@ __device__ void root_step_phase(const UnwDev &d, const uint32_t *roots, uint32_t
             d.pool_hub[base + len] = r;
             d.pool_dist[base + len] = 0;
             d.lab_len[r] = len + 1;
-            d.last_pos[p][r] = base + len;
-            d.last_cnt[p][r] = 1;
+            d.last[p][r] = LastGroup{base + len, 1u, L};
             d.last_min[p][r] = r;
-            d.act_stamp[p][r] = L;
             d.ind_stamp[r] = b + 1;
         }
         __syncwarp();
@@ -297,13 +295,15 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
 
     DBuf<uint8_t> d_used(std::max<uint32_t>(n, 1));
     d_used.upload(used.data(), n, s);
+    if (n) PADO_LAUNCH("heavy_flag_kernel", s, heavy_flag_kernel<<<grid_for(n, 256), 256, 0, s>>>(g.off.p, n, d_used.p));
     uint64_t cap = initial_pool_entries(n);
     DBuf<uint32_t> pool_hub(cap);
     DBuf<uint8_t> pool_dist(cap);
     DBuf<unsigned long long> pool_top(1);
-    DBuf<uint64_t> lab_off(n), last_pos0(n), last_pos1(n);
-    DBuf<uint32_t> lab_len(n), lab_cap(n), last_cnt0(n), last_cnt1(n), last_min0(n), last_min1(n);
-    DBuf<uint32_t> act_stamp0(n), act_stamp1(n), tail_stamp(n), ind_stamp(n);
+    DBuf<uint64_t> lab_off(n);
+    DBuf<LastGroup> last0(n), last1(n);
+    DBuf<uint32_t> lab_len(n), lab_cap(n), last_min0(n), last_min1(n);
+    DBuf<uint32_t> tail_stamp(n), ind_stamp(n);
     DBuf<uint32_t> ind((uint64_t)n * words);
     DBuf<uint8_t> dm((uint64_t)B * n);
     DBuf<uint32_t> front0(n), front1(n), tails(n), htails(n), retry(n), counters(8), status(1);
@@ -312,8 +312,8 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     lab_off.fill_bytes(0, s);
     lab_len.fill_bytes(0, s);
     lab_cap.fill_bytes(0, s);
-    act_stamp0.fill_bytes(0, s);
-    act_stamp1.fill_bytes(0, s);
+    last0.fill_bytes(0, s);  // stamp 0: no group yet
+    last1.fill_bytes(0, s);
     tail_stamp.fill_bytes(0, s);
     ind_stamp.fill_bytes(0, s);
     dm.fill_bytes(0xff, s);
@@ -341,14 +341,10 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     d.lab_off = lab_off.p;
     d.lab_len = lab_len.p;
     d.lab_cap = lab_cap.p;
-    d.last_pos[0] = last_pos0.p;
-    d.last_pos[1] = last_pos1.p;
-    d.last_cnt[0] = last_cnt0.p;
-    d.last_cnt[1] = last_cnt1.p;
+    d.last[0] = last0.p;
+    d.last[1] = last1.p;
     d.last_min[0] = last_min0.p;
     d.last_min[1] = last_min1.p;
-    d.act_stamp[0] = act_stamp0.p;
-    d.act_stamp[1] = act_stamp1.p;
     d.tail_stamp = tail_stamp.p;
     d.ind = ind.p;
     d.ind_stamp = ind_stamp.p;

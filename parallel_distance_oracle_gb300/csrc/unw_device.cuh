@@ -19,11 +19,20 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int SMALL_CAP = 384;                 // labels with d < iter staged in smem per chunk
 constexpr uint32_t HEAVY_DEG = 2048;           // tails this large are processed by a block
 
+// A vertex's label group of one level: list position, size and the level id
+// (stamp) at which it was added -- one 16-byte record, so a reader learns
+// whether a neighbour is active and where its new labels are in one load.
+struct __align__(16) LastGroup {
+    unsigned long long pos;
+    uint32_t cnt;
+    uint32_t stamp;
+};
+
 struct UnwDev {
     uint32_t n, K, B, words;
     const uint32_t *off;
     const uint32_t *adj;
-    const uint8_t *used;
+    const uint8_t *used;    // per vertex: bit 0 BP vertex (never a tail), bit 1 heavy (degree >= HEAVY_DEG)
     const uint8_t *bpd;
     const uint64_t *bps;
     const uint8_t *bpmin;   // per vertex: least BP distance over the roots (255: none)
@@ -34,10 +43,8 @@ struct UnwDev {
     uint64_t *lab_off;
     uint32_t *lab_len;
     uint32_t *lab_cap;
-    uint64_t *last_pos[2];
-    uint32_t *last_cnt[2];
+    LastGroup *last[2];      // by level parity: the vertex's newest label group and its level id
     uint32_t *last_min[2];
-    uint32_t *act_stamp[2];  // by level parity: level id at which the vertex gained labels
     uint32_t *tail_stamp;
     uint32_t *ind;        // n * words
     uint32_t *ind_stamp;  // batch + 1 when the row is valid
@@ -73,6 +80,13 @@ __device__ __forceinline__ uint32_t gd_u32(const uint32_t &f) { return __ldcg(&f
 __device__ __forceinline__ uint64_t gd_u64(const uint64_t &f)
 {
     return (uint64_t)__ldcg(reinterpret_cast<const unsigned long long *>(&f));
+}
+
+// Adds the heavy bit (bit 1) to the per-vertex flags that hold the BP bit.
+__global__ void heavy_flag_kernel(const uint32_t *off, uint32_t n, uint8_t *flags)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        if (off[v + 1] - off[v] >= HEAVY_DEG) flags[v] |= 2u;
 }
 
 // bpmin[v] = least BP distance of v over the K roots (255 if none reaches it).
@@ -153,10 +167,8 @@ __device__ void root_init_phase(const UnwDev &d, const uint32_t *roots, uint32_t
             d.pool_hub[base + len] = r;
             d.pool_dist[base + len] = 0;
             d.lab_len[r] = len + 1;
-            d.last_pos[p][r] = base + len;
-            d.last_cnt[p][r] = 1;
+            d.last[p][r] = LastGroup{base + len, 1u, lid0};
             d.last_min[p][r] = r;
-            d.act_stamp[p][r] = lid0;
             d.ind_stamp[r] = rb + 1;
             front[atomicAdd(front_cnt, 1u)] = r;
         }
@@ -211,9 +223,11 @@ __device__ void mark_phase(const UnwDev &d, const uint32_t *front, uint32_t cnt,
             const bool ok = in && t > mn;
             bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
             bool appended = false;
-            if (ok && !d.used[t] && d.tail_stamp[t] != lid_cur) {
+            const uint32_t f = ok ? d.used[t] : 1u;
+            const uint32_t ts = ok ? d.tail_stamp[t] : lid_cur;
+            if (!(f & 1u) && ts != lid_cur) {
                 if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) {
-                    const bool heavy = d.off[t + 1] - d.off[t] >= HEAVY_DEG;
+                    const bool heavy = f & 2u;
                     if (heavy)
                         htails[agg_append_by(htails_cnt, 1u)] = t;
                     else
@@ -333,24 +347,26 @@ __device__ __forceinline__ bool bp_covered_warp(const UnwDev &d, uint32_t r, int
     return __ballot_sync(FULL, cov) != 0;
 }
 
-// The same test for two candidates at once (rb only if `two`), distances
-// first: a root's 16-byte sets are loaded only where its distance sum can
-// prune (x - 2 <= iter), so sparse graphs, where BP distances are mostly too
-// large, read 64 bytes per candidate instead of 1 KB.  Bit 0: ra covered,
-// bit 1: rb covered.
-__device__ __forceinline__ uint32_t bp_covered_pair(const UnwDev &d, uint32_t ra, uint32_t rb, bool two, int lane,
-                                                    uint32_t skip, uint8_t td0, ulonglong2 ts0, uint8_t td1,
-                                                    ulonglong2 ts1, uint32_t iter)
+// Warp-cooperative BP test of up to BP_GROUP candidates at once (the first
+// `nc` of r[]), distances first: every candidate's distances are loaded in one
+// round, then a root's 16-byte sets only where its distance sum can prune
+// (x - 2 <= iter), in a second round -- sparse graphs, where BP distances are
+// mostly too large, read 64 bytes per candidate instead of 1 KB.  Bit c of the
+// result: r[c] covered.
+constexpr int BP_GROUP = 2;
+__device__ __forceinline__ uint32_t bp_covered_group(const UnwDev &d, const uint32_t (&r)[BP_GROUP], uint32_t nc,
+                                                     int lane, uint32_t skip, uint8_t td0, ulonglong2 ts0, uint8_t td1,
+                                                     ulonglong2 ts1, uint32_t iter)
 {
     const uint32_t K = d.K, i0 = lane, i1 = lane + 32;
     const bool v0 = i0 >= skip && i0 < K, v1 = i1 >= skip && i1 < K;
-    const uint8_t *da = d.bpd + (uint64_t)ra * K, *db = d.bpd + (uint64_t)rb * K;
-    const uint32_t xa0 = v0 ? (uint32_t)da[i0] + td0 : 0u, xa1 = v1 ? (uint32_t)da[i1] + td1 : 0u;
-    const uint32_t xb0 = two && v0 ? (uint32_t)db[i0] + td0 : 0u, xb1 = two && v1 ? (uint32_t)db[i1] + td1 : 0u;
-    // x == 0 (unused lane) fails the test like x < 2 does in bp_one
-    const bool na0 = xa0 - 2u <= iter, na1 = xa1 - 2u <= iter, nb0 = xb0 - 2u <= iter, nb1 = xb1 - 2u <= iter;
-    const ulonglong2 *sa = reinterpret_cast<const ulonglong2 *>(d.bps) + (uint64_t)ra * K;
-    const ulonglong2 *sb = reinterpret_cast<const ulonglong2 *>(d.bps) + (uint64_t)rb * K;
+    uint32_t x0[BP_GROUP], x1[BP_GROUP];
+#pragma unroll
+    for (int c = 0; c < BP_GROUP; ++c) {
+        const uint8_t *rd = d.bpd + (uint64_t)r[c] * K;
+        x0[c] = (uint32_t)c < nc && v0 ? (uint32_t)rd[i0] + td0 : 0u;  // 0: fails the test like x < 2 does
+        x1[c] = (uint32_t)c < nc && v1 ? (uint32_t)rd[i1] + td1 : 0u;
+    }
     auto cut = [&](uint32_t x, ulonglong2 rs, ulonglong2 ts) {
         if (rs.x & ts.x)
             x -= 2u;
@@ -358,12 +374,19 @@ __device__ __forceinline__ uint32_t bp_covered_pair(const UnwDev &d, uint32_t ra
             x -= 1u;
         return x <= iter;
     };
-    bool ca = false, cb = false;
-    if (na0) ca = cut(xa0, sa[i0], ts0);
-    if (na1) ca = ca || cut(xa1, sa[i1], ts1);
-    if (nb0) cb = cut(xb0, sb[i0], ts0);
-    if (nb1) cb = cb || cut(xb1, sb[i1], ts1);
-    return (__ballot_sync(FULL, ca) ? 1u : 0u) | (__ballot_sync(FULL, cb) ? 2u : 0u);
+    bool cov[BP_GROUP];
+#pragma unroll
+    for (int c = 0; c < BP_GROUP; ++c) {
+        const ulonglong2 *rs = reinterpret_cast<const ulonglong2 *>(d.bps) + (uint64_t)r[c] * K;
+        cov[c] = false;
+        if (x0[c] - 2u <= iter) cov[c] = cut(x0[c], rs[i0], ts0);
+        if (x1[c] - 2u <= iter) cov[c] = cov[c] || cut(x1[c], rs[i1], ts1);
+    }
+    uint32_t res = 0;
+#pragma unroll
+    for (int c = 0; c < BP_GROUP; ++c)
+        if (__ballot_sync(FULL, cov[c])) res |= 1u << c;
+    return res;
 }
 
 struct PullArgs {
@@ -423,9 +446,12 @@ __device__ __forceinline__ void mark_tails(const UnwDev &d, uint32_t h, uint32_t
         const bool ok = in && t > mn;
         bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
         bool appended = false;
-        if (ok && !d.used[t] && d.tail_stamp[t] != stamp) {
+        // flags and stamp are independent loads: one round trip
+        const uint32_t f = ok ? d.used[t] : 1u;
+        const uint32_t ts = ok ? d.tail_stamp[t] : stamp;
+        if (!(f & 1u) && ts != stamp) {
             if (atomicExch(&d.tail_stamp[t], stamp) != stamp) {
-                if (d.off[t + 1] - d.off[t] >= HEAVY_DEG)
+                if (f & 2u)
                     htails[agg_append_by(htails_cnt, 1u)] = t;
                 else
                     tails[agg_append_by(tails_cnt, 0u)] = t;
@@ -460,12 +486,13 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         const bool in = e < e_end;
         const uint32_t h = in ? d.adj[e] : 0u;
         const bool ge = in && h >= s;
-        const bool act = ge && d.act_stamp[pp][h] == lid_prev;
+        const LastGroup lg = ge ? d.last[pp][h] : LastGroup{0ull, 0u, 0u};
+        const bool act = ge && lg.stamp == lid_prev;
         uint32_t mask = __ballot_sync(FULL, act);
         if (lane == 0) bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull;
         else { __ballot_sync(FULL, in); __ballot_sync(FULL, ge); }
-        const uint64_t mpos = act ? d.last_pos[pp][h] : 0ull;
-        const uint32_t mcnt = act ? d.last_cnt[pp][h] : 0u;
+        const uint64_t mpos = act ? lg.pos : 0ull;
+        const uint32_t mcnt = act ? lg.cnt : 0u;
         while (mask) {
             const int src = __ffs(mask) - 1;
             mask &= mask - 1;
@@ -618,10 +645,8 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
                 d.lab_cap[t] = hs.ctr[7];
             }
             d.lab_len[t] = len + nadd;
-            d.last_pos[cp][t] = nbase + len;
-            d.last_cnt[cp][t] = nadd;
+            d.last[cp][t] = LastGroup{nbase + len, nadd, a.lid_cur};
             d.last_min[cp][t] = hs.ctr[4];
-            d.act_stamp[cp][t] = a.lid_cur;
             if (!a.next_tails) a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
             bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0) + (hs.ctr[6] ? 10ull * len : 0);
         }
@@ -669,11 +694,12 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         const bool ina = ea < e_end, inb = eb < e_end;
         const uint32_t ha = ina ? d.adj[ea] : 0u, hb = inb ? d.adj[eb] : 0u;
         const bool gea = ina && ha >= s, geb = inb && hb >= s;
-        const bool acta = gea && d.act_stamp[pp][ha] == lid_prev;
-        const bool actb = geb && d.act_stamp[pp][hb] == lid_prev;
-        // every active head's last-group position and size, loaded in parallel
-        const uint64_t pa = acta ? d.last_pos[pp][ha] : 0ull, pb = actb ? d.last_pos[pp][hb] : 0ull;
-        const uint32_t ca = acta ? d.last_cnt[pp][ha] : 0u, cb = actb ? d.last_cnt[pp][hb] : 0u;
+        // every head's newest group (stamp, position, size): one load each, in parallel
+        const LastGroup la = gea ? d.last[pp][ha] : LastGroup{0ull, 0u, 0u};
+        const LastGroup lb = geb ? d.last[pp][hb] : LastGroup{0ull, 0u, 0u};
+        const bool acta = gea && la.stamp == lid_prev, actb = geb && lb.stamp == lid_prev;
+        const uint64_t pa = acta ? la.pos : 0ull, pb = actb ? lb.pos : 0ull;
+        const uint32_t ca = acta ? la.cnt : 0u, cb = actb ? lb.cnt : 0u;
         uint32_t sa = ca, sb = cb;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -740,12 +766,15 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         if (c < noff) {
             const uint16_t idx = wr.offered[c];
             const uint64_t rr = s + idx;
-            if (d.K == 0 || (uint32_t)d.bpmin[rr] + tmin > iter + 2u) {
+            // the three loads are independent: one round trip
+            const uint32_t bm = d.K ? d.bpmin[rr] : (uint32_t)U8_INF;
+            const uint8_t r0d = d.K ? d.bpd[rr * d.K] : (uint8_t)U8_INF;
+            const ulonglong2 r0s = d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K] : zero2;
+            if (d.K == 0 || bm + tmin > iter + 2u) {
                 keep = true;
                 ent = idx | 0x8000u;
             } else {
-                keep = !bp_one(d.bpd[rr * d.K], reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K], tr0d, tr0s,
-                               iter);
+                keep = !bp_one(r0d, r0s, tr0d, tr0s, iter);
                 ent = idx;
             }
         }
@@ -765,15 +794,21 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             uint32_t need = __ballot_sync(FULL, in && !(ent & 0x8000u));
             bool covered = false;
             while (need) {
-                const int ka = __ffs(need) - 1;
-                need &= need - 1;
-                const bool two = need != 0;
-                const int kb = two ? __ffs(need) - 1 : ka;
-                if (two) need &= need - 1;
-                const uint32_t ia = __shfl_sync(FULL, (uint32_t)ent, ka), ib = __shfl_sync(FULL, (uint32_t)ent, kb);
-                const uint32_t cov = bp_covered_pair(d, s + ia, s + ib, two, lane, 1, td0, ts0, td1, ts1, iter);
-                if (lane == ka && (cov & 1u)) covered = true;
-                if (two && lane == kb && (cov & 2u)) covered = true;
+                int kk[BP_GROUP];
+                uint32_t rg[BP_GROUP], nc = 0;
+#pragma unroll
+                for (int g = 0; g < BP_GROUP; ++g) {
+                    kk[g] = need ? __ffs(need) - 1 : 0;
+                    if (need) {
+                        need &= need - 1;
+                        ++nc;
+                    }
+                    rg[g] = s + (__shfl_sync(FULL, (uint32_t)ent, kk[g]) & 0x7fffu);
+                }
+                const uint32_t cov = bp_covered_group(d, rg, nc, lane, 1, td0, ts0, td1, ts1, iter);
+#pragma unroll
+                for (int g = 0; g < BP_GROUP; ++g)
+                    if ((uint32_t)g < nc && lane == kk[g] && (cov >> g & 1u)) covered = true;
             }
             const bool keep = in && !covered;
             const uint32_t km = __ballot_sync(FULL, keep);
@@ -881,10 +916,8 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0);
         if (lane == 0) {
             d.lab_len[t] = len + nadd;
-            d.last_pos[cp][t] = base + len;
-            d.last_cnt[cp][t] = nadd;
+            d.last[cp][t] = LastGroup{base + len, nadd, a.lid_cur};
             d.last_min[cp][t] = mn;
-            d.act_stamp[cp][t] = a.lid_cur;
             if (!a.next_tails) a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
         }
         if (a.next_tails)
