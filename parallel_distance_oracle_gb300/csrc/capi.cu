@@ -218,23 +218,31 @@ int build_common(bool weighted, uint32_t n, const uint64_t *off, const uint32_t 
     return guarded([&] {
         PhaseTrace phase;
         check_build_args(K, B);
-        PADO_CHECK(!weighted || w != nullptr || (off && off[n] == 0), PADO_E_ARG, "null weights");
-        check_graph(n, off, adj);
-        phase("check");
-        if (rank) check_rank(n, rank);
+        PADO_CHECK(off != nullptr, PADO_E_ARG, "null offsets");
+        PADO_CHECK(off[0] == 0, PADO_E_ARG, "off[0] must be 0");
+        PADO_CHECK(off[n] < (1ull << 32), PADO_E_ARG, "more than 2^32-1 adjacency entries");
+        PADO_CHECK(off[n] == 0 || adj != nullptr, PADO_E_ARG, "null adjacency");
+        PADO_CHECK(!weighted || w != nullptr || off[n] == 0, PADO_E_ARG, "null weights");
         std::unique_ptr<pado_index> h = new_index(weighted, n, K, B);
         StreamGuard sg;
         const cudaStream_t s = sg.s;
-        pado::HostGraph hg = pado::relabel_host(n, off, adj, weighted ? w : nullptr, rank);
-        phase("relabel");
-        pado::DevGraph g;
-        upload_graph(hg, g, weighted, s);
-        if (rank) {
-            h->rank.alloc(std::max<uint32_t>(n, 1));
-            h->rank.upload(rank, n, s);
+        // upload, check and (when needed) relabel and sort on the device
+        pado::DevGraph g = pado::prepare_csr(n, off, adj, weighted ? w : nullptr, rank, s, &h->rank);
+        phase("prepare");
+        // root selection reads the offsets and a prefix of the adjacency
+        // (see build_ingested); only those come back to the host
+        pado::HostGraph hg;
+        hg.n = n;
+        hg.off.resize((uint64_t)n + 1);
+        g.off.download(hg.off.data(), (uint64_t)n + 1, s);
+        PADO_CUDA(cudaStreamSynchronize(s));
+        if (!weighted && h->K) {
+            const uint32_t R = (uint32_t)std::min<uint64_t>(n, 65ull * h->K);
+            hg.adj.resize(hg.off[R]);
+            g.adj.download(hg.adj.data(), hg.off[R], s);
+            PADO_CUDA(cudaStreamSynchronize(s));
         }
-        if (phase.on) PADO_CUDA(cudaStreamSynchronize(s));
-        phase("upload");
+        phase("host view");
         label_into(h.get(), hg, g, h->K, B, s, phase);
         *out = h.release();
     });

@@ -488,6 +488,71 @@ __global__ void __launch_bounds__(256) widen_kernel(const uint32_t *a, uint64_t 
         b[i] = a[i];
 }
 
+// ---- CSR input -> ranked CSR -------------------------------------------------
+
+// One warp per vertex: offsets non-decreasing (bit 0), ids < n (bit 1),
+// neighbour lists in descending (id, weight) order (bit 2 clear when not),
+// and the offsets narrowed to 32 bits.
+__global__ void __launch_bounds__(256) csr_check_kernel(const uint64_t *off, const uint32_t *adj, const uint8_t *w,
+                                                        uint32_t n, uint64_t m, uint32_t *off32, uint32_t *flags)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    uint32_t f = 0;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v <= n; v += nw) {
+        if (lane == 0) off32[v] = (uint32_t)off[v];
+        if (v == n) continue;
+        const uint64_t b = off[v], e = off[v + 1];
+        if (e < b || e > m) {  // decreasing somewhere; no entry outside [0, m) is read
+            f |= 1u;
+            continue;
+        }
+        for (uint64_t k = b + lane; k < e; k += 32) {
+            const uint32_t x = adj[k];
+            if (x >= n) f |= 2u;
+            if (k > b) {
+                const uint32_t y = adj[k - 1];
+                if (y < x || (y == x && w && w[k - 1] < w[k])) f |= 4u;
+            }
+        }
+    }
+    if (f) atomicOr(flags, f);
+}
+
+// rank must be a permutation of 0..n-1: seen[] counts each value once.
+__global__ void __launch_bounds__(256) rank_check_kernel(const uint32_t *rank, uint32_t n, uint32_t *seen,
+                                                         uint32_t *flags)
+{
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t r = rank[v];
+        if (r >= n || atomicExch(&seen[r], 1u) != 0u) atomicOr(flags, 8u);
+    }
+}
+
+// Keys of every CSR entry (warp per vertex), the entry_key layout:
+// rank(src) << (b + 8) | (2^b - 1 - rank(dst)) << 8 | (255 - weight).
+__global__ void __launch_bounds__(256) csr_key_kernel(const uint64_t *off, const uint32_t *adj, const uint8_t *w,
+                                                      const uint32_t *rank, uint32_t n, uint32_t bits, uint64_t *keys,
+                                                      uint32_t *degr)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint64_t dmask = (1ull << bits) - 1;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v <= n; v += nw) {
+        if (v == n) {
+            if (lane == 0) degr[n] = 0;
+            continue;
+        }
+        const uint64_t b = off[v], e = off[v + 1];
+        const uint64_t rv = rank ? rank[v] : v;
+        if (lane == 0) degr[rv] = (uint32_t)(e - b);
+        for (uint64_t k = b + lane; k < e; k += 32) {
+            const uint64_t rd = rank ? rank[adj[k]] : adj[k];
+            keys[k] = rv << (bits + 8) | (dmask - rd) << 8 | (255u - (w ? w[k] : 0u));
+        }
+    }
+}
+
 // ---- text -------------------------------------------------------------------
 
 __device__ __forceinline__ bool is_blank(uint8_t c)
@@ -687,6 +752,64 @@ void release_scratch(uint64_t keep_bytes)
 void widen_u32(const uint32_t *a, uint64_t n, uint64_t *b, cudaStream_t s)
 {
     if (n) PADO_LAUNCH("widen_kernel", s, widen_kernel<<<grid_for(n, 256), 256, 0, s>>>(a, n, b));
+}
+
+DevGraph prepare_csr(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, const uint32_t *rank,
+                     cudaStream_t s, DBuf<uint32_t> *rank_out)
+{
+    const uint64_t m = off[n];
+    DevGraph g;
+    g.n = n;
+    g.m = m;
+    g.off.alloc((uint64_t)n + 1);
+    g.adj.alloc(std::max<uint64_t>(m, 1));
+    g.adj.upload(adj, m, s);
+    if (w) {
+        g.w.alloc(std::max<uint64_t>(m, 1));
+        g.w.upload(w, m, s);
+    }
+    PBuf<uint64_t> off64((uint64_t)n + 1, s);
+    PADO_CUDA(cudaMemcpyAsync(off64.p, off, ((uint64_t)n + 1) * 8, cudaMemcpyHostToDevice, s));
+    PBuf<uint32_t> flags(1, s);
+    flags.zero();
+    PADO_LAUNCH("csr_check_kernel", s,
+                csr_check_kernel<<<grid_for(((uint64_t)n + 1) * 32, 256), 256, 0, s>>>(off64.p, g.adj.p,
+                                                                                     w ? g.w.p : nullptr, n, m,
+                                                                                     g.off.p, flags.p));
+    if (rank) {
+        rank_out->alloc(std::max<uint32_t>(n, 1));
+        rank_out->upload(rank, n, s);
+        PBuf<uint32_t> seen(std::max<uint32_t>(n, 1), s);
+        seen.zero();
+        if (n)
+            PADO_LAUNCH("rank_check_kernel", s,
+                        rank_check_kernel<<<grid_for(n, 256), 256, 0, s>>>(rank_out->p, n, seen.p, flags.p));
+    }
+    const uint32_t f = read_back(flags.p, s);
+    PADO_CHECK(!(f & 1u), PADO_E_ARG, "offsets must be non-decreasing");
+    PADO_CHECK(!(f & 2u), PADO_E_ARG, "adjacency id out of range");
+    PADO_CHECK(!(f & 8u), PADO_E_ARG, "rank is not a permutation of 0..n-1");
+    if (!rank && !(f & 4u)) return g;  // ranked and sorted: used as uploaded
+    // relabel by rank and sort every list: the entry sort of the edge-list path
+    const uint32_t bits = id_bits(n);
+    PADO_CHECK(bits <= 28, PADO_E_ARG, "relabeling on the device supports fewer than 2^28 vertices");
+    if (m) {
+        PBuf<uint64_t> keys(m, s);
+        SortSpace ws(m, s);
+        PADO_LAUNCH("csr_key_kernel", s,
+                    csr_key_kernel<<<grid_for(((uint64_t)n + 1) * 32, 256), 256, 0, s>>>(
+                        off64.p, g.adj.p, w ? g.w.p : nullptr, rank ? rank_out->p : nullptr, n, bits, keys.p,
+                        g.off.p));
+        PBuf<uint32_t> osums(scan_sums_needed((uint64_t)n + 1), s);
+        exclusive_scan(g.off.p, (uint64_t)n + 1, osums.p, s);
+        const uint64_t *sorted = radix_sort(keys.p, m, w ? 0u : 8u, 2 * bits + 8, ws, s);
+        PADO_LAUNCH("extract_kernel", s,
+                    extract_kernel<<<grid_for(m, 256), 256, 0, s>>>(sorted, m, bits, g.adj.p, w ? g.w.p : nullptr));
+    } else {
+        g.off.fill_bytes(0, s);
+    }
+    PADO_CUDA(cudaStreamSynchronize(s));
+    return g;
 }
 
 // ---- text parsing -----------------------------------------------------------

@@ -124,6 +124,14 @@ struct IngestResult {  // all on the device
 };
 IngestResult ingest_edges(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, const uint8_t *d_w, uint32_t n,
                           bool dedupe, cudaStream_t s, uint32_t *adj_out = nullptr, uint8_t *w_out = nullptr);
+// CSR input (host arrays: off[n+1] with off[n] < 2^32, adj, optional
+// weights, optional rank over original ids) to the device graph the labelers
+// take, on the device: the offsets, ids and rank are checked there; a ranked
+// CSR whose lists are already descending is used as uploaded, anything else
+// is relabeled and sorted by the entry sort (Graph::id_transfer,
+// graph.h:176-206).  With rank, *rank_out receives it on the device.
+DevGraph prepare_csr(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, const uint32_t *rank,
+                     cudaStream_t s, DBuf<uint32_t> *rank_out);
 // Trims the ingest scratch pool of the current device to keep_bytes.
 void release_scratch(uint64_t keep_bytes);
 // b[i] = a[i] for i < n (device arrays, stream-ordered).

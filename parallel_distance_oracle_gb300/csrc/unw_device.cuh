@@ -221,7 +221,7 @@ __device__ void mark_phase(const UnwDev &d, const uint32_t *front, uint32_t cnt,
             const bool in = e < e_end;
             const uint32_t t = in ? d.adj[e] : 0u;
             const bool ok = in && t > mn;
-            bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
+            if (d.work) bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
             bool appended = false;
             const uint32_t f = ok ? d.used[t] : 1u;
             const uint32_t ts = ok ? d.tail_stamp[t] : lid_cur;
@@ -235,7 +235,7 @@ __device__ void mark_phase(const UnwDev &d, const uint32_t *front, uint32_t cnt,
                     appended = true;
                 }
             }
-            bytes += __popc(__ballot_sync(FULL, appended)) * 8ull;
+            if (d.work) bytes += __popc(__ballot_sync(FULL, appended)) * 8ull;
             if (__ballot_sync(FULL, in && !ok)) break;  // descending: the rest are smaller
         }
     }
@@ -256,7 +256,7 @@ struct WarpRegion {
     uint16_t *offered;    // B
     uint32_t *sh;         // SMALL_CAP
     uint8_t *sd;          // SMALL_CAP
-    uint32_t *ctr;        // [0] noff
+    uint32_t *ctr;        // spare
 };
 
 __host__ __device__ __forceinline__ uint32_t warp_region_bytes(uint32_t words, uint32_t B)
@@ -444,7 +444,7 @@ __device__ __forceinline__ void mark_tails(const UnwDev &d, uint32_t h, uint32_t
         const bool in = e < e_end;
         const uint32_t t = in ? d.adj[e] : 0u;
         const bool ok = in && t > mn;
-        bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
+        if (d.work) bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
         bool appended = false;
         // flags and stamp are independent loads: one round trip
         const uint32_t f = ok ? d.used[t] : 1u;
@@ -458,9 +458,11 @@ __device__ __forceinline__ void mark_tails(const UnwDev &d, uint32_t h, uint32_t
                 appended = true;
             }
         }
-        const uint32_t na = __popc(__ballot_sync(FULL, appended));
-        bytes += na * 8ull;
-        if (gcnt && na && lane == 0) atomicAdd(gcnt, na);  // the head's graph's tails for this stamp
+        if (gcnt || d.work) {
+            const uint32_t na = __popc(__ballot_sync(FULL, appended));
+            bytes += na * 8ull;
+            if (gcnt && na && lane == 0) atomicAdd(gcnt, na);  // the head's graph's tails for this stamp
+        }
         if (__ballot_sync(FULL, in && !ok)) break;
     }
 }
@@ -681,7 +683,7 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     // (a) indicator row of t for this batch
     const bool valid = d.ind_stamp[t] == bc.b + 1;
     for (uint32_t x = lane; x < d.words; x += 32) wr.ind[x] = valid ? d.ind[(uint64_t)t * d.words + x] : 0u;
-    if (lane == 0) wr.ctr[0] = 0;
+    uint32_t noff = 0;  // first offers so far, in wr.offered
     __syncwarp();
     // (b) gather first offers from active neighbours (heads >= s), 64
     // neighbours per step.  The hubs of all active heads' last groups are
@@ -710,7 +712,8 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             }
         }
         const uint32_t ta = __shfl_sync(FULL, sa, 31), tot = ta + __shfl_sync(FULL, sb, 31);
-        bytes += __popc(__ballot_sync(FULL, ina)) * 4ull + __popc(__ballot_sync(FULL, gea)) * 4ull +
+        if (d.work)
+            bytes += __popc(__ballot_sync(FULL, ina)) * 4ull + __popc(__ballot_sync(FULL, gea)) * 4ull +
                  __popc(__ballot_sync(FULL, inb)) * 4ull + __popc(__ballot_sync(FULL, geb)) * 4ull +
                  12ull * (__popc(__ballot_sync(FULL, acta)) + __popc(__ballot_sync(FULL, actb))) + 4ull * tot;
         for (uint32_t i0 = 0; i0 < tot; i0 += 32) {
@@ -726,21 +729,25 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             }
             const uint64_t qa = __shfl_sync(FULL, pa, L), qb = __shfl_sync(FULL, pb, L);
             const uint32_t xa = __shfl_sync(FULL, sa - ca, L), xb = __shfl_sync(FULL, sb - cb, L);
+            bool fresh = false;
+            uint32_t idx = 0;
             if (i < tot) {
                 const uint32_t r = d.pool_hub[(second ? qb : qa) + (key - (second ? xb : xa))];
                 if (r < t) {
-                    const uint32_t idx = r - s;
+                    idx = r - s;
                     const uint32_t bit = 1u << (idx & 31);
-                    const uint32_t old = atomicOr(&wr.ind[idx >> 5], bit);
-                    if (!(old & bit)) wr.offered[atomicAdd(&wr.ctr[0], 1u)] = (uint16_t)idx;
+                    fresh = !(atomicOr(&wr.ind[idx >> 5], bit) & bit);
                 }
             }
+            // first offers of this round appended in lane order (no shared counter)
+            const uint32_t fm = __ballot_sync(FULL, fresh);
+            if (fresh) wr.offered[noff + __popc(fm & ((1u << lane) - 1u))] = (uint16_t)idx;
+            noff += __popc(fm);
         }
         // descending list: once a neighbour is < s, the rest are too
         if (__ballot_sync(FULL, (ina && !gea) || (inb && !geb))) break;
     }
     __syncwarp();
-    const uint32_t noff = wr.ctr[0];
     tick(W_CYC_SCAN);
     if (noff == 0) return;
     bytes += 17ull * d.K + 4ull * d.words + 4;  // tail BP row; indicator write-back
@@ -752,8 +759,6 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     const ulonglong2 ts0 = lane < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane] : zero2;
     const ulonglong2 ts1 =
         lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
-    const uint8_t tr0d = __shfl_sync(FULL, td0, 0);
-    const ulonglong2 tr0s = make_ulonglong2(__shfl_sync(FULL, ts0.x, 0), __shfl_sync(FULL, ts0.y, 0));
     // Any root i gives td_i >= bpmin[r] + bpmin[t], so a pair with
     // bpmin[r] + bpmin[t] - 2 > iter cannot be covered: it survives BP without
     // a row load (flag 0x8000: no second stage).
@@ -766,15 +771,18 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         if (c < noff) {
             const uint16_t idx = wr.offered[c];
             const uint64_t rr = s + idx;
-            // the three loads are independent: one round trip
+            // the candidate's and the tail's root-0 entries (the latter the same
+            // address in every lane) are independent loads: one round trip
             const uint32_t bm = d.K ? d.bpmin[rr] : (uint32_t)U8_INF;
             const uint8_t r0d = d.K ? d.bpd[rr * d.K] : (uint8_t)U8_INF;
             const ulonglong2 r0s = d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K] : zero2;
+            const uint8_t t0d = d.K ? d.bpd[(uint64_t)t * d.K] : (uint8_t)U8_INF;
+            const ulonglong2 t0s = d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K] : zero2;
             if (d.K == 0 || bm + tmin > iter + 2u) {
                 keep = true;
                 ent = idx | 0x8000u;
             } else {
-                keep = !bp_one(r0d, r0s, tr0d, tr0s, iter);
+                keep = !bp_one(r0d, r0s, t0d, t0s, iter);
                 ent = idx;
             }
         }
@@ -824,8 +832,9 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     }
     tick(W_CYC_BP);
     // (d) distance test against t's labels with d < iter.  Those labels are
-    // staged in shared memory SMALL_CAP at a time (ballot compaction, in list
-    // order); when they all fit, one staging serves every candidate group.
+    // staged in shared memory as (hub, slack = iter - d) SMALL_CAP at a time
+    // (ballot compaction, in list order); when they all fit, one staging
+    // serves every candidate group.
     uint32_t nadd = 0;
     const uint32_t len = d.lab_len[t];
     uint64_t base = d.lab_off[t];
@@ -843,7 +852,7 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
                 if (sm) {
                     const uint32_t p = cnt + __popc(m & ((1u << lane) - 1u));
                     wr.sh[p] = d.pool_hub[base + jj];
-                    wr.sd[p] = dd;
+                    wr.sd[p] = (uint8_t)(iter - dd);  // slack: covered iff d(r, h) <= slack
                 }
                 cnt += __popc(m);
             }
@@ -869,20 +878,18 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
                     for (; k + 4 <= nst; k += 4) {
                         const uint32_t h0 = wr.sh[k], h1 = wr.sh[k + 1], h2 = wr.sh[k + 2], h3 = wr.sh[k + 3];
                         const uint32_t v0 = row[h0], v1 = row[h1], v2 = row[h2], v3 = row[h3];
-                        if ((h0 < rr && (uint32_t)wr.sd[k] + v0 <= iter) ||
-                            (h1 < rr && (uint32_t)wr.sd[k + 1] + v1 <= iter) ||
-                            (h2 < rr && (uint32_t)wr.sd[k + 2] + v2 <= iter) ||
-                            (h3 < rr && (uint32_t)wr.sd[k + 3] + v3 <= iter)) {
+                        if ((h0 < rr && v0 <= wr.sd[k]) || (h1 < rr && v1 <= wr.sd[k + 1]) ||
+                            (h2 < rr && v2 <= wr.sd[k + 2]) || (h3 < rr && v3 <= wr.sd[k + 3])) {
                             keep = false;
                             break;
                         }
                     }
                     for (; keep && k < nst; ++k) {
                         const uint32_t hh = wr.sh[k];
-                        if (hh < rr && (uint32_t)wr.sd[k] + (uint32_t)row[hh] <= iter) keep = false;
+                        if (hh < rr && (uint32_t)row[hh] <= wr.sd[k]) keep = false;
                     }
                 }
-                bytes += (uint64_t)__popc(__ballot_sync(FULL, c < nsurv)) * nst;
+                if (d.work) bytes += (uint64_t)__popc(__ballot_sync(FULL, c < nsurv)) * nst;
                 if (whole || next >= len || !__any_sync(FULL, keep)) break;
                 next = stage(next);
             }

@@ -54,18 +54,20 @@ def test_too_many_bp_roots_rejected():
     assert _build_status(K=65)[0] == 1
 
 
-def test_bad_rank_rejected():
+def test_bad_offsets_rejected():
     g = G.path_graph(6)
-    r = np.array([0, 1, 2, 3, 4, 4], np.uint32)
-    assert _build_status(g=g, rank=r)[0] == 1
-    assert b"permutation" in _lib.lib.pado_last_error()
-
-
-def test_bad_adjacency_rejected():
-    g = G.path_graph(6)
-    g.adj = g.adj.copy()
-    g.adj[0] = 99
+    g.off = g.off.copy()
+    g.off[0] = 1
     assert _build_status(g=g)[0] == 1
+    assert b"off[0]" in _lib.lib.pado_last_error()
+    g = G.path_graph(6)
+    g.off = g.off.copy()
+    g.off[-1] = 1 << 33
+    assert _build_status(g=g)[0] == 1
+
+
+# Rank permutations and adjacency ids are checked on the device (where the
+# CSR is uploaded): tests/test_gpu_parity.py covers them.
 
 
 def test_missing_index_file_is_io_error(tmp_path):

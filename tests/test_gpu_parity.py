@@ -235,3 +235,54 @@ def test_pool_growth_retry_path_is_exact(pado, monkeypatch):
     rw = G.degree_rank(gw)
     _, lw = gpu_w(pado, gw, rw, 128)
     assert_same_w(lw, orc.w_label(gw, rw, 128), "tiny pool weighted")
+
+
+def test_device_input_checks(pado):
+    """Offsets, adjacency ids and the rank permutation are checked on the
+    device after the upload; each bad input fails with PADO_E_ARG."""
+    from parallel_distance_oracle_gb300 import _lib
+    g = G.path_graph(6)
+    bad_rank = np.array([0, 1, 2, 3, 4, 4], np.uint32)
+    with pytest.raises(_lib.PadoError, match="permutation"):
+        pado.VertexCentricPLL(g, bad_rank, bp_roots=2, batch=4)
+    with pytest.raises(_lib.PadoError, match="permutation"):
+        pado.VertexCentricPLL(g, np.array([0, 1, 2, 3, 4, 6], np.uint32), bp_roots=2, batch=4)
+    b = G.CSRGraph(n=g.n, off=g.off, adj=g.adj.copy())
+    b.adj[0] = 99
+    with pytest.raises(_lib.PadoError, match="out of range"):
+        pado.VertexCentricPLL(b, G.degree_rank(g), bp_roots=2, batch=4)
+    with pytest.raises(_lib.PadoError, match="out of range"):
+        pado.VertexCentricPLL(b, None, bp_roots=2, batch=4)
+    off = g.off.copy()
+    off[3] = off[4] + 1  # decreasing at vertex 3
+    with pytest.raises(_lib.PadoError, match="non-decreasing"):
+        pado.VertexCentricPLL(G.CSRGraph(n=g.n, off=off, adj=g.adj), None, bp_roots=2, batch=4)
+    w = G.rmat(8, 4, 3, weights=(1, 9))
+    wb = G.CSRGraph(n=w.n, off=w.off, adj=w.adj.copy(), w=w.w)
+    wb.adj[-1] = w.n
+    with pytest.raises(_lib.PadoError, match="out of range"):
+        pado.WeightedVertexCentricPLL(wb, G.degree_rank(w), batch=8)
+
+
+def test_unsorted_ranked_input_is_sorted_on_the_device(pado):
+    """A ranked CSR whose lists are not descending is sorted on the device
+    and labels like the sorted one (weights follow their entries)."""
+    g = G.rmat(10, 8, 9, weights=(1, 50))
+    rk = G.degree_rank(g)
+    src = np.repeat(np.arange(g.n), np.diff(g.off).astype(np.int64))
+    ns, nd = rk[src].astype(np.int64), rk[g.adj].astype(np.int64)
+    rng = np.random.Generator(np.random.PCG64(2))
+    o = np.lexsort((rng.random(len(nd)), ns))  # grouped by source, lists shuffled
+    off = np.zeros(g.n + 1, np.uint64)
+    np.cumsum(np.bincount(ns, minlength=g.n), out=off[1:])
+    shuffled = G.CSRGraph(g.n, off, nd[o].astype(np.uint32), g.w[o])
+    a = pado.WeightedVertexCentricPLL(shuffled, None, batch=64).export()
+    b = pado.WeightedVertexCentricPLL(g, rk, batch=64)
+    b.order_labels(rank=np.arange(g.n, dtype=np.uint32))  # compare keyed by rank on both sides
+    b = b.export()
+    assert np.array_equal(a.off, b.off) and np.array_equal(a.hub, b.hub) and np.array_equal(a.dist, b.dist)
+    ua = pado.VertexCentricPLL(G.CSRGraph(g.n, off, nd[o].astype(np.uint32)), None, bp_roots=8, batch=64).export()
+    ub = pado.VertexCentricPLL(g, rk, bp_roots=8, batch=64)
+    ub.order_labels(rank=np.arange(g.n, dtype=np.uint32))
+    ub = ub.export()
+    assert np.array_equal(ua.off, ub.off) and np.array_equal(ua.hub, ub.hub) and np.array_equal(ua.bps, ub.bps)
