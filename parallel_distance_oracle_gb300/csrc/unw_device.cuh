@@ -750,20 +750,16 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     __syncwarp();
     tick(W_CYC_SCAN);
     if (noff == 0) return;
-    bytes += 17ull * d.K + 4ull * d.words + 4;  // tail BP row; indicator write-back
+    bytes += 17ull + 4ull * d.words + 4;  // tail root-0 BP entry; indicator write-back
     // (c) BP test in two stages: lane per candidate on BP root 0 (which settles
     // most pairs), then warp-cooperative over the remaining roots for the rest.
     const ulonglong2 zero2 = make_ulonglong2(0, 0);
-    const uint8_t td0 = lane < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane] : (uint8_t)U8_INF;
-    const uint8_t td1 = lane + 32 < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane + 32] : (uint8_t)U8_INF;
-    const ulonglong2 ts0 = lane < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane] : zero2;
-    const ulonglong2 ts1 =
-        lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
     // Any root i gives td_i >= bpmin[r] + bpmin[t], so a pair with
     // bpmin[r] + bpmin[t] - 2 > iter cannot be covered: it survives BP without
     // a row load (flag 0x8000: no second stage).
     const uint32_t tmin = d.K ? d.bpmin[t] : (uint32_t)U8_INF;
     uint32_t nsurv = 0;
+    bool need2 = false;  // some survivor needs the second stage
     for (uint32_t c0 = 0; c0 < noff; c0 += 32) {
         const uint32_t c = c0 + lane;
         bool keep = false;
@@ -787,13 +783,22 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             }
         }
         const uint32_t km = __ballot_sync(FULL, keep);
+        need2 = need2 || __any_sync(FULL, keep && !(ent & 0x8000u));
         __syncwarp();
         if (keep) wr.offered[nsurv + __popc(km & ((1u << lane) - 1u))] = ent;
         nsurv += __popc(km);
         __syncwarp();
     }
-    if (d.K > 1 && nsurv) {
-        // second stage for the unflagged survivors, two candidates per step
+    if (d.K > 1 && need2) {
+        // second stage for the unflagged survivors, two candidates per step,
+        // against t's whole row (lane i: roots i and i + 32), loaded only now
+        const uint8_t td0 = lane < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane] : (uint8_t)U8_INF;
+        const uint8_t td1 = lane + 32 < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane + 32] : (uint8_t)U8_INF;
+        const ulonglong2 ts0 =
+            lane < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane] : zero2;
+        const ulonglong2 ts1 =
+            lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
+        bytes += 17ull * (d.K - 1);
         uint32_t n2 = 0;
         for (uint32_t c0 = 0; c0 < nsurv; c0 += 32) {
             const uint32_t c = c0 + lane;
