@@ -109,6 +109,7 @@ struct LoopCtl {
     GridBar bar;
     uint32_t phase, b, iter, lid;       // the step to run next: phase, batch, level, last completed stamp
     uint32_t tcnt[3], hcnt[3];          // light / heavy tails marked for stamp x, in slot x % 3
+    uint32_t tq[3], hq[3];              // work counters of the level at stamp x (dynamic assignment)
     uint32_t rr_cnt, retry_cnt, status, exit_code;
     uint32_t levels, pad;
 };
@@ -189,6 +190,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 4) label_loop_kernel(UnwDev d, L
             if (leader) {
                 c->tcnt[(L + 2) % 3] = 0;
                 c->hcnt[(L + 2) % 3] = 0;
+                c->tq[(L + 2) % 3] = 0;
+                c->hq[(L + 2) % 3] = 0;
             }
             if (!grid_barrier(&c->bar, &c->status)) return;
             if (vload(&c->retry_cnt)) {
@@ -233,10 +236,14 @@ __global__ void __launch_bounds__(PULL_THREADS, 4) label_loop_kernel(UnwDev d, L
         a.next_htails_cnt = &c->hcnt[nx];
         a.next_stamp = L + 1;
         a.dm = bf.dm[b & 1];
+        a.tail_q = &c->tq[cur];
+        a.htail_q = &c->hq[cur];
         pull_phase(d, a, pull_smem);
         if (leader && phase == PH_LEVEL) {
             c->tcnt[(L + 2) % 3] = 0;
             c->hcnt[(L + 2) % 3] = 0;
+            c->tq[(L + 2) % 3] = 0;
+            c->hq[(L + 2) % 3] = 0;
         }
         if (!grid_barrier(&c->bar, &c->status)) return;
         if (vload(&c->retry_cnt)) {
@@ -469,6 +476,7 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
                     h.tcnt[cur] = h.retry_cnt;
                     h.hcnt[cur] = 0;
                 }
+                for (int x = 0; x < 3; ++x) h.tq[x] = h.hq[x] = 0;  // the re-run level claims from zero
                 h.retry_cnt = 0;
                 h.status = 0;
                 h.exit_code = EX_RUNNING;

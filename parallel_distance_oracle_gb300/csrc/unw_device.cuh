@@ -297,7 +297,7 @@ struct HeavyRegion {
     uint16_t *offered;
     uint16_t *surv;
     uint8_t *sd;
-    uint32_t *ctr;                   // noff, nsurv, nsmall, nadd, mn, ok, reloc, ncap
+    uint32_t *ctr;                   // noff, nsurv, nsmall, nadd, mn, ok, reloc, ncap, nsurv2
     unsigned long long *base;
 };
 
@@ -409,6 +409,11 @@ struct PullArgs {
     uint32_t *next_htails = nullptr, *next_htails_cnt = nullptr;
     uint32_t next_stamp = 0;
     uint8_t *dm = nullptr;           // dist_matrix of the current batch (default d.dm)
+    // Work counters for dynamic assignment (zero at the start of the level):
+    // warps / blocks claim the next light / heavy tail from them, so that the
+    // level ends when the work runs out rather than when the unluckiest
+    // static share is done.  Null: static grid-stride assignment.
+    uint32_t *tail_q = nullptr, *htail_q = nullptr;
 };
 
 // The batch a tail belongs to: roots [s, e), batch id b, level iter, and its
@@ -478,7 +483,7 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     const uint32_t lid_prev = a.lid_cur - 1;
     const bool valid = d.ind_stamp[t] == bc.b + 1;
     for (uint32_t x = tid; x < d.words; x += blockDim.x) hs.ind[x] = valid ? d.ind[(uint64_t)t * d.words + x] : 0u;
-    if (tid < 8) hs.ctr[tid] = (tid == 4) ? 0xffffffffu : 0u;
+    if (tid < 9) hs.ctr[tid] = (tid == 4) ? 0xffffffffu : 0u;
     if (tid == 0) bytes += 8 + 8ull * d.words;
     __syncthreads();
     // (a) first offers from active neighbours, warps striding over the list
@@ -537,26 +542,27 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             hs.surv[atomicAdd(&hs.ctr[1], 1u)] = idx;
     }
     __syncthreads();
+    // every thread reads the count before anything changes it; the second
+    // stage counts its survivors in a slot of its own (ctr[8])
     const uint32_t nsurv1 = hs.ctr[1];
+    uint32_t nsurv = nsurv1;
     if (d.K > 1 && nsurv1) {
-        if (tid == 0) hs.ctr[1] = 0;
-        __syncthreads();
         for (uint32_t c = warp; c < nsurv1; c += blockDim.x >> 5) {
             const uint16_t ent = hs.surv[c];
             const uint16_t idx = ent & 0x7fffu;
             const bool cov = !(ent & 0x8000u) && bp_covered_warp(d, s + idx, lane, 1, td0, ts0, td1, ts1, iter);
-            if (!cov && lane == 0) hs.offered[atomicAdd(&hs.ctr[1], 1u)] = idx;
+            if (!cov && lane == 0) hs.offered[atomicAdd(&hs.ctr[8], 1u)] = idx;
         }
         __syncthreads();
         // survivors now sit in `offered`; move them back for the distance test
-        const uint32_t ns2 = hs.ctr[1];
+        const uint32_t ns2 = hs.ctr[8];
         for (uint32_t c = tid; c < ns2; c += blockDim.x) hs.surv[c] = hs.offered[c];
         __syncthreads();
+        nsurv = ns2;
     } else {
         for (uint32_t c = tid; c < nsurv1; c += blockDim.x) hs.surv[c] &= 0x7fffu;
         __syncthreads();
     }
-    const uint32_t nsurv = hs.ctr[1];
     const uint32_t len = d.lab_len[t];
     const uint64_t base = d.lab_off[t];
     // (c) distance test
@@ -949,20 +955,59 @@ __device__ void pull_phase(const UnwDev &d, const PullArgs &a, unsigned char *pu
     const int lane = threadIdx.x & 31;
     unsigned long long bytes = 0;
     const uint32_t hcnt = a.htails_cnt ? *a.htails_cnt : 0u;
+    const uint32_t cnt = *a.tails_cnt;
+    if (a.tail_q && hcnt + cnt <= gridDim.x) {
+        // a small level: every tail gets a whole block (the heavy path), so
+        // that its scan and tests spread over 8 warps instead of one
+        HeavyRegion hs = heavy_region(pull_smem, d.words, d.B);
+        for (uint32_t q = blockIdx.x; q < hcnt + cnt; q += gridDim.x) {
+            pull_heavy_tail(d, a, q < hcnt ? a.htails[q] : a.tails[q - hcnt], hs, bytes);
+            __syncthreads();
+        }
+        if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_PULL], bytes);
+        __syncthreads();
+        return;
+    }
     if (hcnt) {
         const long long h0 = d.work ? clock64() : 0;
         HeavyRegion hs = heavy_region(pull_smem, d.words, d.B);
-        for (uint32_t q = blockIdx.x; q < hcnt; q += gridDim.x) {
-            pull_heavy_tail(d, a, a.htails[q], hs, bytes);
-            __syncthreads();
+        if (a.htail_q) {
+            __shared__ uint32_t hq;
+            for (;;) {
+                if (threadIdx.x == 0) hq = atomicAdd(a.htail_q, 1u);
+                __syncthreads();
+                const uint32_t q = hq;
+                __syncthreads();
+                if (q >= hcnt) break;
+                pull_heavy_tail(d, a, a.htails[q], hs, bytes);
+                __syncthreads();
+            }
+        } else {
+            for (uint32_t q = blockIdx.x; q < hcnt; q += gridDim.x) {
+                pull_heavy_tail(d, a, a.htails[q], hs, bytes);
+                __syncthreads();
+            }
         }
         if (d.work && threadIdx.x == 0) atomicAdd(&d.work[W_CYC_HEAVY], (unsigned long long)(clock64() - h0));
     }
-    const uint32_t cnt = *a.tails_cnt;
     WarpRegion wr = warp_region(pull_smem, d.words, d.B, threadIdx.x >> 5);
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw)
-        pull_light_tail(d, a, a.tails[q], wr, bytes);
+    if (a.tail_q) {
+        // the next claim is issued before the current tail is processed, so
+        // its latency is hidden; each warp over-claims once at the end
+        uint32_t q = 0;
+        if (lane == 0) q = atomicAdd(a.tail_q, 1u);
+        q = __shfl_sync(FULL, q, 0);
+        while (q < cnt) {
+            uint32_t nq = 0;
+            if (lane == 0) nq = atomicAdd(a.tail_q, 1u);
+            pull_light_tail(d, a, a.tails[q], wr, bytes);
+            q = __shfl_sync(FULL, nq, 0);
+        }
+    } else {
+        const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+        for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw)
+            pull_light_tail(d, a, a.tails[q], wr, bytes);
+    }
     if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_PULL], bytes);
     __syncthreads();
 }
