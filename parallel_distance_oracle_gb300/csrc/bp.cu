@@ -46,6 +46,7 @@ constexpr unsigned FULL_MASK = 0xffffffffu;
 constexpr uint32_t HEAVY = 2048;     // vertices worked on by a whole block
 constexpr int BP_THREADS = 256;
 constexpr int BP_WARPS = BP_THREADS / 32;
+constexpr int NB = 4;                // neighbours whose rows are loaded together
 
 // Slots where a vertex is on level `lvl`; valid only if `lvl` matches the level
 // being read (the two parity buffers are never cleared).
@@ -108,14 +109,31 @@ __device__ __forceinline__ void sibling_range(const MsState &st, uint32_t v, uns
         unsigned long long common = fv & fu;
         uint32_t mask = __ballot_sync(FULL_MASK, common != 0);
         bytes += 20ull * __popc(__ballot_sync(FULL_MASK, in));
+        // NB neighbours per round, their rows loaded before any is ORed in
         while (mask) {
-            const int k = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const uint32_t uk = __shfl_sync(FULL_MASK, u, k);
-            const unsigned long long ck = __shfl_sync(FULL_MASK, common, k);
-            if ((ck >> lane) & 1ull) acc0 |= st.bps[(uint64_t)uk * st.K + lane].x;
-            if ((ck >> (lane + 32)) & 1ull) acc1 |= st.bps[(uint64_t)uk * st.K + lane + 32].x;
-            bytes += 8ull * __popcll(ck);
+            uint32_t uk[NB];
+            unsigned long long ck[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                const int k = mask ? __ffs(mask) - 1 : 0;
+                const bool has = mask != 0;
+                if (has) mask &= mask - 1;
+                uk[j] = __shfl_sync(FULL_MASK, u, k);
+                const unsigned long long cc = __shfl_sync(FULL_MASK, common, k);
+                ck[j] = has ? cc : 0ull;
+            }
+            unsigned long long x0[NB], x1[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                x0[j] = (ck[j] >> lane) & 1ull ? st.bps[(uint64_t)uk[j] * st.K + lane].x : 0ull;
+                x1[j] = (ck[j] >> (lane + 32)) & 1ull ? st.bps[(uint64_t)uk[j] * st.K + lane + 32].x : 0ull;
+            }
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                acc0 |= x0[j];
+                acc1 |= x1[j];
+                bytes += 8ull * __popcll(ck[j]);
+            }
         }
     }
 }
@@ -136,23 +154,35 @@ __device__ __forceinline__ void child_range(const MsState &st, uint32_t w, unsig
         const unsigned long long m = in ? (level_bits(st, u, d) & ~rw) : 0ull;
         uint32_t mask = __ballot_sync(FULL_MASK, m != 0);
         bytes += 20ull * __popc(__ballot_sync(FULL_MASK, in));
+        // NB neighbours per round, their rows loaded before any is ORed in
         while (mask) {
-            const int k = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const uint32_t uk = __shfl_sync(FULL_MASK, u, k);
-            const unsigned long long mk = __shfl_sync(FULL_MASK, m, k);
-            newm |= mk;
-            if ((mk >> lane) & 1ull) {
-                const ulonglong2 x = st.bps[(uint64_t)uk * st.K + lane];
-                a0.x |= x.x;
-                a0.y |= x.y;
+            uint32_t uk[NB];
+            unsigned long long mk[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                const int k = mask ? __ffs(mask) - 1 : 0;
+                const bool has = mask != 0;
+                if (has) mask &= mask - 1;
+                uk[j] = __shfl_sync(FULL_MASK, u, k);
+                const unsigned long long mm = __shfl_sync(FULL_MASK, m, k);
+                mk[j] = has ? mm : 0ull;
             }
-            if ((mk >> (lane + 32)) & 1ull) {
-                const ulonglong2 x = st.bps[(uint64_t)uk * st.K + lane + 32];
-                a1.x |= x.x;
-                a1.y |= x.y;
+            const ulonglong2 z = make_ulonglong2(0, 0);
+            ulonglong2 x0[NB], x1[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                x0[j] = (mk[j] >> lane) & 1ull ? st.bps[(uint64_t)uk[j] * st.K + lane] : z;
+                x1[j] = (mk[j] >> (lane + 32)) & 1ull ? st.bps[(uint64_t)uk[j] * st.K + lane + 32] : z;
             }
-            bytes += 16ull * __popcll(mk);
+#pragma unroll
+            for (int j = 0; j < NB; ++j) {
+                newm |= mk[j];
+                a0.x |= x0[j].x;
+                a0.y |= x0[j].y;
+                a1.x |= x1[j].x;
+                a1.y |= x1[j].y;
+                bytes += 16ull * __popcll(mk[j]);
+            }
         }
     }
 }

@@ -76,12 +76,17 @@ int guarded(F &&f)
     }
 }
 
+// Set on threads that already run one of several parallel workers (the
+// union builder's): their loops stay serial instead of spawning threads of
+// their own.
+thread_local bool t_serial = false;
+
 // Run f(lo, hi) over [0, n) on the host's cores (plain threads, no OpenMP).
 template <typename F>
 void parallel_ranges(uint32_t n, F &&f)
 {
     unsigned T = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-    if (n < 4096 || T == 1) {
+    if (n < 4096 || T == 1 || t_serial) {
         f(0u, n);
         return;
     }
@@ -337,6 +342,7 @@ UnionGraph union_graph(uint32_t G, const uint32_t *n, const uint64_t *const *off
     std::vector<std::string> errs(T);
     for (unsigned t = 0; t < T; ++t)
         th.emplace_back([&, t] {
+            t_serial = true;
             try {
                 for (size_t i = t; i < pick.size(); i += T) {
                     const uint32_t gi = pick[i], ng = n[gi], base = u.gbase[i];
@@ -737,9 +743,11 @@ int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *of
         PADO_CHECK(G >= 1 && G <= 65535, PADO_E_ARG, "between 1 and 65535 graphs");
         PADO_CHECK(batch >= 1 && batch <= pado::MAX_BATCH, PADO_E_ARG, "batch size must be in [1, 2048]");
         PADO_CHECK(bp_roots <= pado::MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
+        PhaseTrace phase;
         std::vector<uint32_t> pick(G);
         std::iota(pick.begin(), pick.end(), 0u);
         UnionGraph u = union_graph(G, n, off, adj, rank, pick);
+        phase("union");
         int dev = 0;
         PADO_CUDA(cudaGetDevice(&dev));
         cudaStream_t s;
@@ -747,13 +755,18 @@ int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *of
         struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
         ManyRun r;
         many_bp(u, bp_roots, r, s);
+        phase("bit-parallel");
         pado::LabelStore all;
         pado::LabelRun run = pado::unw_label_many(r.g, u.gbase, bp_roots, batch, r.used, r.bpd.p, r.bps.p, all, s);
+        phase("labeling");
         const uint32_t N = u.hg.n;
         std::vector<uint64_t> fo(N + 1);
         all.off.download(fo.data(), N + 1, s);
         PADO_CUDA(cudaStreamSynchronize(s));
         const uint32_t K = bp_roots;
+        // every graph's offsets, rebased to its own list start, in one host
+        // array that outlives the uploads (one synchronisation at the end)
+        std::vector<uint64_t> lo_all((uint64_t)N + G);
         for (uint32_t i = 0; i < G; ++i) {
             const uint32_t base = u.gbase[i], ng = n[i];
             std::unique_ptr<pado_index> h(new pado_index);
@@ -767,11 +780,11 @@ int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *of
                 h->rank.upload(rank[i], ng, s);
             }
             const uint64_t l0 = fo[base], tot = fo[base + ng] - l0;
-            std::vector<uint64_t> lo(ng + 1);
+            uint64_t *lo = lo_all.data() + base + i;  // ng + 1 entries
             for (uint32_t v = 0; v <= ng; ++v) lo[v] = fo[base + v] - l0;
             h->store.total = tot;
             h->store.off.alloc(ng + 1);
-            h->store.off.upload(lo.data(), ng + 1, s);
+            h->store.off.upload(lo, ng + 1, s);
             h->store.hub.alloc(std::max<uint64_t>(tot, 1));
             h->store.dist8.alloc(std::max<uint64_t>(tot, 1));
             if (tot) {
@@ -786,8 +799,6 @@ int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *of
                 PADO_CUDA(cudaMemcpyAsync(h->bps.p, r.bps.p + (uint64_t)base * K * 2, (uint64_t)ng * K * 16,
                                           cudaMemcpyDeviceToDevice, s));
             }
-            // lo[] must stay alive until its upload has run
-            PADO_CUDA(cudaStreamSynchronize(s));
             h->info.n = ng;
             h->info.kind = PADO_UNWEIGHTED;
             h->info.bp_roots = K;
@@ -800,6 +811,8 @@ int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *of
             h->info.device_bytes = h->device_bytes();
             hs[i] = std::move(h);
         }
+        PADO_CUDA(cudaStreamSynchronize(s));  // lo_all and the copies
+        phase("split");
     });
     if (st == PADO_OK)
         for (uint32_t i = 0; i < G; ++i) out[i] = hs[i].release();

@@ -248,6 +248,7 @@ __device__ void mark_phase(const UnwDev &d, const uint32_t *front, uint32_t cnt,
 constexpr int PULL_THREADS = 256;
 constexpr int PULL_NW = PULL_THREADS / 32;
 constexpr int HSMALL_CAP = 1024;          // heavy tail: labels with d < iter staged
+constexpr uint32_t SMALL_LEVEL_PER_BLOCK = 1;  // levels with at most this many tails per block use the block path
 
 __host__ __device__ __forceinline__ uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
 
@@ -956,7 +957,7 @@ __device__ void pull_phase(const UnwDev &d, const PullArgs &a, unsigned char *pu
     unsigned long long bytes = 0;
     const uint32_t hcnt = a.htails_cnt ? *a.htails_cnt : 0u;
     const uint32_t cnt = *a.tails_cnt;
-    if (a.tail_q && hcnt + cnt <= gridDim.x) {
+    if (a.tail_q && hcnt + cnt <= SMALL_LEVEL_PER_BLOCK * gridDim.x) {
         // a small level: every tail gets a whole block (the heavy path), so
         // that its scan and tests spread over 8 warps instead of one
         HeavyRegion hs = heavy_region(pull_smem, d.words, d.B);

@@ -50,6 +50,7 @@ struct ManyCtl {
     GridBar bar;
     uint32_t phase, lid, active, steps;
     uint32_t tcnt[3], hcnt[3];  // light / heavy tails marked for stamp x, in slot x % 3
+    uint32_t tq[3], hq[3];      // work counters of the step at stamp x (dynamic assignment)
     uint32_t rq_cnt[2];         // roots to start in step L: rq[L & 1]
     uint32_t zq_cnt[2];         // roots whose dist_matrix rows are reset in step L
     uint32_t rr_cnt, rretry_cnt, tretry_cnt, status, exit_code, pad;
@@ -192,6 +193,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 4) many_loop_kernel(UnwDev d, Ma
         a.next_htails = bf.htails[nx];
         a.next_htails_cnt = &c->hcnt[nx];
         a.next_stamp = L + 1;
+        a.tail_q = &c->tq[cur];
+        a.htail_q = &c->hq[cur];
         if (phase == MP_STEP) {
             dm_rows_phase(d, bf.zq[cp], vload(&c->zq_cnt[cp]), 0u, 0, bf.gd, bf.gmap);
             many_root_step(d, bf, c, bf.rq[cp], vload(&c->rq_cnt[cp]), L);
@@ -202,6 +205,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 4) many_loop_kernel(UnwDev d, Ma
         if (leader) {
             c->tcnt[(L + 2) % 3] = 0;
             c->hcnt[(L + 2) % 3] = 0;
+            c->tq[(L + 2) % 3] = 0;
+            c->hq[(L + 2) % 3] = 0;
         }
         if (!grid_barrier(&c->bar, &c->status)) return;
         if (vload(&c->rretry_cnt) || vload(&c->tretry_cnt)) {
@@ -433,6 +438,7 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
                 PADO_CUDA(cudaMemcpyAsync(lists[cur], tretry.p, h.tretry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
                 h.tcnt[cur] = h.tretry_cnt;
                 h.hcnt[cur] = 0;
+                for (int x = 0; x < 3; ++x) h.tq[x] = h.hq[x] = 0;  // the re-run step claims from zero
                 h.rretry_cnt = 0;
                 h.tretry_cnt = 0;
                 h.status = 0;
