@@ -776,23 +776,23 @@ int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *of
             h->K = K;
             h->B = batch;
             if (rank && rank[i]) {
-                h->rank.alloc(std::max<uint32_t>(ng, 1));
+                h->rank.alloc_async(std::max<uint32_t>(ng, 1), s);
                 h->rank.upload(rank[i], ng, s);
             }
             const uint64_t l0 = fo[base], tot = fo[base + ng] - l0;
             uint64_t *lo = lo_all.data() + base + i;  // ng + 1 entries
             for (uint32_t v = 0; v <= ng; ++v) lo[v] = fo[base + v] - l0;
             h->store.total = tot;
-            h->store.off.alloc(ng + 1);
+            h->store.off.alloc_async(ng + 1, s);
             h->store.off.upload(lo, ng + 1, s);
-            h->store.hub.alloc(std::max<uint64_t>(tot, 1));
-            h->store.dist8.alloc(std::max<uint64_t>(tot, 1));
+            h->store.hub.alloc_async(std::max<uint64_t>(tot, 1), s);
+            h->store.dist8.alloc_async(std::max<uint64_t>(tot, 1), s);
             if (tot) {
                 PADO_CUDA(cudaMemcpyAsync(h->store.hub.p, all.hub.p + l0, tot * 4, cudaMemcpyDeviceToDevice, s));
                 PADO_CUDA(cudaMemcpyAsync(h->store.dist8.p, all.dist8.p + l0, tot, cudaMemcpyDeviceToDevice, s));
             }
-            h->bpd.alloc(std::max<uint64_t>((uint64_t)ng * K, 1));
-            h->bps.alloc(std::max<uint64_t>((uint64_t)ng * K * 2, 1));
+            h->bpd.alloc_async(std::max<uint64_t>((uint64_t)ng * K, 1), s);
+            h->bps.alloc_async(std::max<uint64_t>((uint64_t)ng * K * 2, 1), s);
             if ((uint64_t)ng * K) {
                 PADO_CUDA(cudaMemcpyAsync(h->bpd.p, r.bpd.p + (uint64_t)base * K, (uint64_t)ng * K,
                                           cudaMemcpyDeviceToDevice, s));

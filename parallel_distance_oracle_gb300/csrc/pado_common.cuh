@@ -62,6 +62,15 @@ struct DBuf {
         if (count) PADO_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
         n = count;
     }
+    // Stream-ordered allocation from the device's default memory pool (cheap
+    // when many small buffers are made at once); cudaFree releases it like
+    // any other.
+    void alloc_async(size_t count, cudaStream_t s)
+    {
+        release();
+        if (count) PADO_CUDA(cudaMallocAsync((void **)&p, count * sizeof(T), s));
+        n = count;
+    }
     void release()
     {
         if (p) cudaFree(p);
