@@ -339,7 +339,8 @@ void pado_server_destroy(pado_server *s);
 
 /* Enable (1) or disable (0) per-kernel timing: while enabled every launch is
  * bracketed by CUDA events on its stream and hot kernels count their
- * algorithmic bytes.  Adds overhead; for profiling runs only. */
+ * algorithmic bytes.  Adds overhead; for profiling runs only.  2 times the
+ * launches without the byte counters (whose atomics slow the hot kernels). */
 int pado_profile(int enable);
 
 /* Write the profile table as text lines "kernel launches total_ms bytes" into

@@ -78,7 +78,7 @@ bool profiling() { return g_profile.load(std::memory_order_relaxed) != 0; }
 
 unsigned long long *work_counters()
 {
-    return profiling() ? g_work : nullptr;
+    return g_profile.load(std::memory_order_relaxed) == 1 ? g_work : nullptr;
 }
 
 void prof_begin(cudaStream_t s)
@@ -121,7 +121,7 @@ int pado_profile(int enable)
         cudaMemset(pado::g_work, 0, pado::WORK_SLOTS * sizeof(unsigned long long));
     }
     if (!enable) pado::collect_locked();
-    pado::g_profile.store(enable ? 1 : 0);
+    pado::g_profile.store(enable == 2 ? 2 : enable ? 1 : 0);
     return PADO_OK;
 }
 
