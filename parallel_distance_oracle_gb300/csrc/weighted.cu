@@ -213,11 +213,13 @@ __global__ void w_snap_kernel(WDev d, uint32_t rows) { w_snap_phase(d, rows); }
 
 // Per-warp dynamic shared memory: rmin[B] int32, res[B] int32, touched[B] u16.
 // Run by blocks of WPULL_WARPS warps.
+// tq: the round's work counter for dynamic tail claiming (null: static
+// grid-stride assignment).
 __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt, uint32_t s, uint32_t b,
                              uint32_t lid_cur, uint32_t *front_next, uint32_t *front_next_cnt, uint32_t *news,
-                             uint32_t *news_cnt, uint32_t *retry, uint32_t *retry_cnt, unsigned char *wsm)
+                             uint32_t *news_cnt, uint32_t *retry, uint32_t *retry_cnt, unsigned char *wsm,
+                             uint32_t *tq = nullptr)
 {
-    __shared__ uint32_t s_cnt[WPULL_WARPS][2];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const uint32_t B = d.B;
@@ -232,46 +234,66 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
     for (uint32_t c = lane; c < B; c += 32) rmin[c] = RMIN_EMPTY;
     __syncwarp();
     unsigned long long bytes = 0;
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw) {
-        const uint32_t t = tails[q];
+    const uint32_t below = (1u << lane) - 1u;
+    auto pull_tail = [&](const uint32_t t) {
         bytes += 8;
-        if (lane == 0) s_cnt[w][0] = 0;
-        __syncwarp();
-        // (a) round minimum of the relaxations arriving at t, per root
+        // (a) round minimum of the relaxations arriving at t, per root.  The
+        // active heads' logged roots are flattened into one item list over
+        // the lanes (inclusive counts sa), so one round of loads covers 32
+        // entries whichever heads they belong to.
+        uint32_t ntouch = 0;  // roots touched so far, in `touched`
         const uint32_t e_end = d.off[t + 1];
         for (uint32_t e0 = d.off[t]; e0 < e_end; e0 += 32) {
             const uint32_t e = e0 + lane;
             const bool in = e < e_end;
             const uint32_t h = in ? d.adj[e] : 0u;
             const bool ge = in && h >= s;
-            const bool act = ge && d.act_stamp[pp][h] == lid_prev;
+            // stamp, log position and size of every head: independent loads
+            const uint32_t st = ge ? d.act_stamp[pp][h] : 0u;
+            const uint64_t hp = ge ? d.last_pos[pp][h] : 0ull;
+            const uint32_t hc = ge ? d.last_cnt[pp][h] : 0u;
+            const bool act = ge && st == lid_prev;
             const int32_t wt = act ? (int32_t)d.w[e] : 0;
-            uint32_t mask = __ballot_sync(FULL, act);
-            bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull +
-                     __popc(mask) * 13ull;
-            while (mask) {
-                const int src = __ffs(mask) - 1;
-                mask &= mask - 1;
-                const uint32_t hh = __shfl_sync(FULL, h, src);
-                const int32_t ww = __shfl_sync(FULL, wt, src);
-                const uint64_t pos = d.last_pos[pp][hh];
-                const uint32_t c = d.last_cnt[pp][hh];
-                bytes += 4ull * c;
-                for (uint32_t j = lane; j < c; j += 32) {
-                    const uint32_t x = d.log[pp][pos + j];
-                    const uint32_t cr = x >> 16;
+            const uint32_t ca = act ? hc : 0u;
+            const uint64_t pa = act ? hp : 0ull;
+            uint32_t sa = ca;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, sa, o);
+                if (lane >= o) sa += y;
+            }
+            const uint32_t tot = __shfl_sync(FULL, sa, 31);
+            if (d.work)
+                bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull +
+                         __popc(__ballot_sync(FULL, act)) * 13ull + 4ull * tot;
+            for (uint32_t i0 = 0; i0 < tot; i0 += 32) {
+                const uint32_t i = i0 + lane;
+                uint32_t L = 0;  // head lane: the lanes whose inclusive count is <= i
+#pragma unroll
+                for (uint32_t step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(FULL, sa, L + step - 1) <= i) L += step;
+                const uint64_t qp = __shfl_sync(FULL, pa, L);
+                const uint32_t x0 = __shfl_sync(FULL, sa - ca, L);
+                const int32_t ww = __shfl_sync(FULL, wt, L);
+                bool fresh = false;
+                uint32_t cr = 0;
+                if (i < tot) {
+                    const uint32_t x = d.log[pp][qp + (i - x0)];
+                    cr = x >> 16;
                     if (s + cr < t) {
                         const int32_t m = (int32_t)(int16_t)((int32_t)(int16_t)(x & 0xffffu) + ww);
-                        const int32_t old = atomicMin(&rmin[cr], m);
-                        if (old == RMIN_EMPTY) touched[atomicAdd(&s_cnt[w][0], 1u)] = (uint16_t)cr;
+                        fresh = atomicMin(&rmin[cr], m) == RMIN_EMPTY;
                     }
                 }
+                // first touches of this round appended in lane order
+                const uint32_t fm = __ballot_sync(FULL, fresh);
+                if (fresh) touched[ntouch + __popc(fm & below)] = (uint16_t)cr;
+                ntouch += __popc(fm);
             }
             if (__ballot_sync(FULL, in && !ge)) break;
         }
         __syncwarp();
-        const uint32_t ntouch = s_cnt[w][0];
-        if (ntouch == 0) continue;
+        if (ntouch == 0) return;
         // (b) candidates: round minimum below dists_table; checks (1) and (2)
         const uint64_t cbase = d.lab_off[t];
         const uint32_t clen = d.lab_len[t];
@@ -364,11 +386,9 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
                 }
                 for (uint32_t i = lane; i < ntouch; i += 32) rmin[touched[i]] = RMIN_EMPTY;
                 __syncwarp();
-                continue;
+                return;
             }
         }
-        if (lane == 0) s_cnt[w][1] = 0;
-        __syncwarp();
         uint32_t accb = 0, newb = 0;
         for (uint32_t i0 = 0; i0 < ntouch; i0 += 32) {
             const uint32_t i = i0 + lane;
@@ -416,6 +436,21 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
             }
         }
         __syncwarp();
+    };
+    if (tq) {
+        // dynamic claiming: the next claim is issued before the current tail
+        // is processed; each warp over-claims once at the end
+        uint32_t q = 0;
+        if (lane == 0) q = atomicAdd(tq, 1u);
+        q = __shfl_sync(FULL, q, 0);
+        while (q < cnt) {
+            uint32_t nq = 0;
+            if (lane == 0) nq = atomicAdd(tq, 1u);
+            pull_tail(tails[q]);
+            q = __shfl_sync(FULL, nq, 0);
+        }
+    } else {
+        for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw) pull_tail(tails[q]);
     }
     if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_WPULL], bytes);
 }
@@ -580,6 +615,7 @@ struct WLoopCtl {
     uint32_t phase, b, lid, cur;      // resume point: phase, batch, last stamp, front parity
     uint32_t rounds, levels;
     uint32_t front_cnt[2], tails_cnt[2], news_cnt[2];
+    uint32_t tq[2];                   // the pull's work counter, by the round's tails slot
     uint32_t rr_cnt, retry_cnt, status, exit_code;
 };
 
@@ -618,7 +654,10 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
             // front[cur], news[b & 1] and log[lid0 & 1] were cleared at the end of the previous batch
             w_root_init_phase(d, s, nr, lid0, bf.front[cur], &c->front_cnt[cur], bf.news[b & 1],
                               &c->news_cnt[b & 1]);
-            if (leader) c->tails_cnt[(lid0 + 1) & 1] = 0;  // the first round's tails
+            if (leader) {
+                c->tails_cnt[(lid0 + 1) & 1] = 0;  // the first round's tails
+                c->tq[(lid0 + 1) & 1] = 0;
+            }
             if (!grid_barrier(&c->bar, &c->status)) return;
             lid = lid0;
             rounds = 0;
@@ -640,10 +679,11 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
                 if (!grid_barrier(&c->bar, &c->status)) return;
             }
             w_pull_phase(d, bf.tails[tp], vload(&c->tails_cnt[tp]), s, b, lid_cur, bf.front[nxt], &c->front_cnt[nxt],
-                         bf.news[b & 1], &c->news_cnt[b & 1], bf.retry, &c->retry_cnt, wsm);
+                         bf.news[b & 1], &c->news_cnt[b & 1], bf.retry, &c->retry_cnt, wsm, &c->tq[tp]);
             if (leader) {
                 c->front_cnt[cur] = 0;             // consumed by this round's mark
                 c->tails_cnt[(lid_cur + 1) & 1] = 0;  // read by the previous round's pull
+                c->tq[(lid_cur + 1) & 1] = 0;
             }
             if (!grid_barrier(&c->bar, &c->status)) return;
             if (vload(&c->retry_cnt)) {
@@ -864,6 +904,7 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
                     uint32_t *tl[2] = {tails.p, tails2.p};
                     PADO_CUDA(cudaMemcpyAsync(tl[tp], retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
                     h.tails_cnt[tp] = h.retry_cnt;
+                    h.tq[0] = h.tq[1] = 0;  // the re-run pull claims from zero
                 } else {
                     PADO_CHECK(h.exit_code == WX_NEED_POOL, PADO_E_STATE, "weighted labeling loop stopped unexpectedly");
                     unsigned long long top = 0;
