@@ -202,10 +202,15 @@ inline uint64_t initial_pool_entries(uint32_t n)
     const uint64_t dbg = debug_pool_entries();
     return dbg ? dbg : std::min<uint64_t>(std::max<uint64_t>((uint64_t)n * 256, 1u << 22), 1ull << 31);
 }
+// The weighted round logs start at 128 entries per vertex (1 KB per vertex
+// for both parities): the busiest rounds of the first batch of a social graph
+// accept that many roots per vertex, and every growth stops the persistent
+// loop once.
 inline uint64_t initial_log_entries(uint32_t n, uint32_t B)
 {
     const uint64_t dbg = debug_pool_entries();
-    return dbg ? std::max<uint64_t>(dbg, B) : std::max<uint64_t>((uint64_t)n * 4, (uint64_t)B + (1u << 16));
+    return dbg ? std::max<uint64_t>(dbg, B)
+               : std::min<uint64_t>(std::max<uint64_t>((uint64_t)n * 128, (uint64_t)B + (1u << 16)), 1ull << 31);
 }
 
 }  // namespace pado

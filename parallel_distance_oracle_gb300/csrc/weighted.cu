@@ -845,7 +845,7 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
     };
     // Grow both round logs (the one being written and the one being read).
     auto grow_logs = [&](unsigned long long need) {
-        uint64_t ncap = std::max<uint64_t>(lcap * 2, need + need / 2);
+        uint64_t ncap = std::max<uint64_t>(lcap * 4, 2 * need);  // a growth costs a relaunch: grow far
         DBuf<uint32_t> n0(ncap), n1(ncap);
         PADO_CUDA(cudaMemcpyAsync(n0.p, log0.p, lcap * 4, cudaMemcpyDeviceToDevice, s));
         PADO_CUDA(cudaMemcpyAsync(n1.p, log1.p, lcap * 4, cudaMemcpyDeviceToDevice, s));
@@ -893,6 +893,9 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
                 PADO_CUDA(cudaStreamSynchronize(s));
                 if (h.status & ST_BARRIER_TIMEOUT)
                     throw Error(PADO_E_TIMEOUT, "weighted labeling loop: a grid barrier timed out");
+                if (std::getenv("PADO_TRACE"))
+                    fprintf(stderr, "weighted loop launch %d: exit %u at batch %u (retry %u)\n", launch, h.exit_code,
+                            h.b, h.retry_cnt);
                 if (h.exit_code == WX_DONE) break;
                 if (h.exit_code == WX_STALL) throw Error(PADO_E_STATE, "relaxation did not converge");
                 if (h.exit_code == WX_NEED_LOG) {
