@@ -305,7 +305,10 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
     DBuf<uint8_t> d_used(std::max<uint32_t>(n, 1));
     d_used.upload(used.data(), n, s);
     if (n) PADO_LAUNCH("heavy_flag_kernel", s, heavy_flag_kernel<<<grid_for(n, 256), 256, 0, s>>>(g.off.p, n, d_used.p));
-    uint64_t cap = initial_pool_entries(n);
+    // Many small graphs carry more labels per vertex than one large sparse
+    // one, and every growth stops the loop: start at 3x the one-graph pool.
+    uint64_t cap = debug_pool_entries() ? initial_pool_entries(n)
+                                        : std::min<uint64_t>(3 * initial_pool_entries(n), 1ull << 31);
     DBuf<uint32_t> pool_hub(cap);
     DBuf<uint8_t> pool_dist(cap);
     DBuf<unsigned long long> pool_top(1);
