@@ -8,8 +8,9 @@
 //   td -= 2 / 1 / 0 by the S^-1 / S^0 intersections and d = min(d, td);
 //   then d = min over common hubs h of dist_a(h) + dist_b(h); saturate.
 // Lane i evaluates BP roots i and i+32 (K <= 64), and the two hub-sorted label
-// lists are intersected 32 x 32 entries at a time with warp shuffles,
-// advancing the block whose last hub is smaller.  The result is a warp
+// lists are intersected 32 x 32 entries at a time: each lane binary-searches
+// its a-hub among the b-block with warp shuffles, and the block whose last
+// hub is smaller advances.  The result is a warp
 // min-reduction.  Everything is integer arithmetic with the reference's
 // unsigned comparisons, so results are bit-exact.
 #pragma once
@@ -43,14 +44,17 @@ __device__ __forceinline__ uint32_t intersect_min(const uint32_t *__restrict__ h
         const uint32_t bv = vb ? __ldg(hb + ib + lane) : 0xfffffffeu;
         const uint32_t ad = va ? (uint32_t)(int32_t)da[ia + lane] : 0u;
         const uint32_t bd = vb ? (uint32_t)(int32_t)db[ib + lane] : 0u;
-#pragma unroll 8
-        for (int j = 0; j < 32; ++j) {
-            const uint32_t x = __shfl_sync(FULL, bv, j);
-            const uint32_t y = __shfl_sync(FULL, bd, j);
-            if (x == av) {
-                const uint32_t td = ad + y;
-                d = td < d ? td : d;
-            }
+        // each a-hub finds its place in the (sorted) b-chunk by a binary
+        // search over the lanes: 5 shuffles instead of comparing all 32
+        uint32_t lo = 0;
+#pragma unroll
+        for (uint32_t step = 16; step > 0; step >>= 1)
+            if (__shfl_sync(FULL, bv, lo + step - 1) < av) lo += step;
+        const uint32_t x = __shfl_sync(FULL, bv, lo);
+        const uint32_t y = __shfl_sync(FULL, bd, lo);
+        if (va && x == av) {
+            const uint32_t td = ad + y;
+            d = td < d ? td : d;
         }
         const uint32_t amax = __shfl_sync(FULL, av, (int)(ra < 32 ? ra - 1 : 31));
         const uint32_t bmax = __shfl_sync(FULL, bv, (int)(rb < 32 ? rb - 1 : 31));
