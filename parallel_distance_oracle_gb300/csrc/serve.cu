@@ -105,6 +105,105 @@ struct Req {
     double t_arrival = 0, t_done = 0;
 };
 
+// One staging copy: caller memory <-> page-locked slot memory.
+struct CopyJob {
+    void *dst;
+    const void *src;
+    uint64_t bytes;
+};
+
+// Helper threads that split a batch's staging copies.  A full batch moves 8
+// bytes per pair from callers' pageable arrays into page-locked staging (2 MiB
+// at 2^18 pairs) and the results back; one host core copies about 10 GB/s,
+// which would cap the loop below what the GPU answers.  Lists under MIN_SPLIT
+// bytes are copied by the calling thread alone.
+class CopyCrew {
+public:
+    explicit CopyCrew(unsigned helpers) : nhelp_(helpers)
+    {
+        for (unsigned i = 0; i < helpers; ++i) th_.emplace_back([this, i] { loop(i); });
+    }
+    ~CopyCrew()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (std::thread &t : th_) t.join();
+    }
+    // Performs every job; the calling thread copies the last share itself.
+    void run(const std::vector<CopyJob> &jobs)
+    {
+        uint64_t total = 0;
+        for (const CopyJob &j : jobs) total += j.bytes;
+        if (!nhelp_ || total < MIN_SPLIT) {
+            copy_range(jobs, 0, total);
+            return;
+        }
+        const unsigned parts = nhelp_ + 1;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            jobs_ = &jobs;
+            total_ = total;
+            pending_ = nhelp_;
+            ++gen_;
+        }
+        cv_.notify_all();
+        copy_range(jobs, total * nhelp_ / parts, total);
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [&] { return pending_ == 0; });
+        jobs_ = nullptr;
+    }
+
+private:
+    static constexpr uint64_t MIN_SPLIT = 256ull << 10;
+
+    // bytes [lo, hi) of the jobs laid end to end
+    static void copy_range(const std::vector<CopyJob> &jobs, uint64_t lo, uint64_t hi)
+    {
+        uint64_t at = 0;
+        for (const CopyJob &j : jobs) {
+            if (at >= hi) break;
+            const uint64_t a = std::max(lo, at), b = std::min(hi, at + j.bytes);
+            if (a < b)
+                memcpy(static_cast<unsigned char *>(j.dst) + (a - at),
+                       static_cast<const unsigned char *>(j.src) + (a - at), b - a);
+            at += j.bytes;
+        }
+    }
+
+    void loop(unsigned i)
+    {
+        uint64_t seen = 0;
+        for (;;) {
+            const std::vector<CopyJob> *jobs;
+            uint64_t total;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                jobs = jobs_;
+                total = total_;
+            }
+            const unsigned parts = nhelp_ + 1;
+            copy_range(*jobs, total * i / parts, total * (i + 1) / parts);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--pending_ == 0) done_.notify_one();
+        }
+    }
+
+    const unsigned nhelp_;
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::vector<CopyJob> *jobs_ = nullptr;
+    uint64_t total_ = 0, gen_ = 0;
+    unsigned pending_ = 0;
+    bool stop_ = false;
+};
+
 struct Slot {
     HBuf<uint32_t> ha, hb;
     HBuf<unsigned char> hout;
@@ -121,6 +220,7 @@ struct Slot {
     };
     std::vector<Item> items;
     std::vector<uint32_t> used;   // indexes this batch reads (in-flight references)
+    std::vector<CopyJob> copies;  // staging copies of the batch being filled or retired
 };
 
 struct Entry {
@@ -134,6 +234,8 @@ struct Entry {
 }  // namespace
 }  // namespace pado
 
+using pado::CopyCrew;
+using pado::CopyJob;
 using pado::Entry;
 using pado::Req;
 using pado::Slot;
@@ -155,6 +257,7 @@ struct pado_server {
     cudaStream_t admin = nullptr;
     pado_server_stats st{};
     std::string fatal;             // a CUDA error that stopped the dispatcher
+    std::unique_ptr<CopyCrew> crew;  // splits the dispatcher's staging copies
 
     void run();
     bool acquire(uint32_t i, Slot &sl, pado::IndexView *v, bool *weighted);
@@ -247,10 +350,14 @@ void pado_server::release(Slot &sl)
 
 void pado_server::complete(Slot &sl)
 {
-    for (const Slot::Item &it : sl.items) {
-        memcpy(static_cast<unsigned char *>(it.r->out) + it.off * it.esz, sl.hout.p + it.out_pos, it.len * it.esz);
+    sl.copies.clear();
+    for (const Slot::Item &it : sl.items)
+        sl.copies.push_back({static_cast<unsigned char *>(it.r->out) + it.off * it.esz, sl.hout.p + it.out_pos,
+                             it.len * it.esz});
+    crew->run(sl.copies);
+    sl.copies.clear();
+    for (const Slot::Item &it : sl.items)
         if (--it.r->chunks_out == 0 && it.r->next == it.r->k) finish(this, it.r, PADO_OK);
-    }
     release(sl);
     sl.items.clear();
 }
@@ -260,6 +367,7 @@ bool pado_server::dispatch(Slot &sl)
 {
     uint64_t pairs = 0, out_bytes = 0;
     uint32_t nrun = 0;
+    sl.copies.clear();
     for (;;) {
         Req *r = nullptr;
         {
@@ -285,8 +393,9 @@ bool pado_server::dispatch(Slot &sl)
         const uint32_t esz = weighted ? 2u : 1u;
         const uint64_t take = std::min<uint64_t>(r->k - r->next, max_pairs - pairs);
         out_bytes = (out_bytes + 1) & ~1ull;  // int16 results start 2-byte aligned
-        memcpy(sl.ha.p + pairs, r->a + r->next, take * 4);
-        memcpy(sl.hb.p + pairs, r->b + r->next, take * 4);
+        // the request's arrays stay valid until it completes, which is after this batch retires
+        sl.copies.push_back({sl.ha.p + pairs, r->a + r->next, take * 4});
+        sl.copies.push_back({sl.hb.p + pairs, r->b + r->next, take * 4});
         pado::ServeRun &run = sl.hrun.p[nrun++];
         run.start = pairs;
         run.out_off = out_bytes;
@@ -307,6 +416,8 @@ bool pado_server::dispatch(Slot &sl)
         release(sl);  // a set admitted for a request that did not fit
         return false;
     }
+    crew->run(sl.copies);
+    sl.copies.clear();
     sl.hrun.p[0].v.work = pado::work_counters();
     PADO_CUDA(cudaMemcpyAsync(sl.da.p, sl.ha.p, pairs * 4, cudaMemcpyHostToDevice, sl.s));
     PADO_CUDA(cudaMemcpyAsync(sl.db.p, sl.hb.p, pairs * 4, cudaMemcpyHostToDevice, sl.s));
@@ -424,6 +535,8 @@ int pado_server_create(uint64_t hbm_budget_bytes, uint32_t max_batch_pairs, uint
             PADO_CUDA(cudaStreamCreateWithFlags(&sl.s, cudaStreamNonBlocking));
             PADO_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
         }
+        // helpers for the staging copies: a quarter of the host threads, at most 4
+        S->crew.reset(new CopyCrew(std::min(4u, std::thread::hardware_concurrency() / 4)));
         pado_server *raw = S.get();
         S->worker = std::thread([raw] { raw->run(); });
         *out = S.release();
