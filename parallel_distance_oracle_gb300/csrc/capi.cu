@@ -7,6 +7,7 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <thread>
 
@@ -1004,6 +1005,43 @@ int pado_query_device(pado_index *h, uint64_t k, const uint32_t *d_a, const uint
     });
 }
 
+namespace {
+
+// Pairs per chunk of the host query path.
+constexpr uint64_t QUERY_CHUNK = 1ull << 21;
+
+// The second stream of the chunked host query path: one per device, created
+// on first use and kept for the life of the process.
+cudaStream_t query_aux_stream(int dev)
+{
+    static std::mutex mu;
+    static std::vector<std::pair<int, cudaStream_t>> streams;
+    std::lock_guard<std::mutex> lk(mu);
+    for (const auto &e : streams)
+        if (e.first == dev) return e.second;
+    cudaStream_t s = nullptr;
+    PADO_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    streams.emplace_back(dev, s);
+    return s;
+}
+
+void launch_query(const pado_index *h, uint64_t k, const uint32_t *da, const uint32_t *db, void *dout,
+                  cudaStream_t s)
+{
+    if (h->kind == PADO_UNWEIGHTED)
+        pado::launch_query_unw(h->view(), k, da, db, static_cast<uint8_t *>(dout), s);
+    else
+        pado::launch_query_w(h->view(), k, da, db, static_cast<int16_t *>(dout), s);
+}
+
+}  // namespace
+
+// Host arrays in, host array out.  Up to QUERY_CHUNK pairs: copy in, one
+// launch, copy out.  Beyond that the pairs go in chunks alternating between
+// two streams, and chunk c's results are copied out only after chunk c + 1 is
+// queued: a copy out to pageable memory returns when it has completed, and
+// with the next chunk's kernel already queued on the other stream the GPU
+// keeps working while the host copies (and stages the chunk after).
 int pado_query(pado_index *h, uint64_t k, const uint32_t *a, const uint32_t *b, void *out)
 {
     if (!h || (k && (!a || !b || !out))) return fail(PADO_E_ARG, "null argument");
@@ -1016,22 +1054,59 @@ int pado_query(pado_index *h, uint64_t k, const uint32_t *a, const uint32_t *b, 
         void *buf = nullptr;
         PADO_CUDA(cudaMallocAsync(&buf, k * (8 + osz), s));
         uint32_t *da = static_cast<uint32_t *>(buf), *db = da + k;
-        void *dout = db + k;
+        unsigned char *dout = reinterpret_cast<unsigned char *>(db + k);
+        if (k <= QUERY_CHUNK) {
+            try {
+                PADO_CUDA(cudaMemcpyAsync(da, a, k * 4, cudaMemcpyHostToDevice, s));
+                PADO_CUDA(cudaMemcpyAsync(db, b, k * 4, cudaMemcpyHostToDevice, s));
+                launch_query(h, k, da, db, dout, s);
+                PADO_CUDA(cudaMemcpyAsync(out, dout, k * osz, cudaMemcpyDeviceToHost, s));
+                PADO_CUDA(cudaFreeAsync(buf, s));
+                PADO_CUDA(cudaStreamSynchronize(s));
+            } catch (...) {
+                cudaFreeAsync(buf, s);
+                cudaStreamSynchronize(s);
+                throw;
+            }
+            return;
+        }
+        cudaStream_t s2 = nullptr;
+        cudaEvent_t ev[2] = {nullptr, nullptr};
         try {
-            PADO_CUDA(cudaMemcpyAsync(da, a, k * 4, cudaMemcpyHostToDevice, s));
-            PADO_CUDA(cudaMemcpyAsync(db, b, k * 4, cudaMemcpyHostToDevice, s));
-            if (h->kind == PADO_UNWEIGHTED)
-                pado::launch_query_unw(h->view(), k, da, db, static_cast<uint8_t *>(dout), s);
-            else
-                pado::launch_query_w(h->view(), k, da, db, static_cast<int16_t *>(dout), s);
-            PADO_CUDA(cudaMemcpyAsync(out, dout, k * osz, cudaMemcpyDeviceToHost, s));
+            s2 = query_aux_stream(h->device);
+            PADO_CUDA(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+            PADO_CUDA(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+            PADO_CUDA(cudaEventRecord(ev[0], s));  // the buffer exists for s2 too
+            PADO_CUDA(cudaStreamWaitEvent(s2, ev[0], 0));
+            const cudaStream_t st[2] = {s, s2};
+            const uint64_t nch = (k + QUERY_CHUNK - 1) / QUERY_CHUNK;
+            auto back = [&](uint64_t c) {
+                const uint64_t lo = c * QUERY_CHUNK, n = std::min(QUERY_CHUNK, k - lo);
+                PADO_CUDA(cudaMemcpyAsync(static_cast<unsigned char *>(out) + lo * osz, dout + lo * osz, n * osz,
+                                          cudaMemcpyDeviceToHost, st[c & 1]));
+            };
+            for (uint64_t c = 0; c < nch; ++c) {
+                const uint64_t lo = c * QUERY_CHUNK, n = std::min(QUERY_CHUNK, k - lo);
+                PADO_CUDA(cudaMemcpyAsync(da + lo, a + lo, n * 4, cudaMemcpyHostToDevice, st[c & 1]));
+                PADO_CUDA(cudaMemcpyAsync(db + lo, b + lo, n * 4, cudaMemcpyHostToDevice, st[c & 1]));
+                launch_query(h, n, da + lo, db + lo, dout + lo * osz, st[c & 1]);
+                if (c) back(c - 1);
+            }
+            back(nch - 1);
+            PADO_CUDA(cudaEventRecord(ev[1], s2));  // s2's chunks are done before the buffer is freed
+            PADO_CUDA(cudaStreamWaitEvent(s, ev[1], 0));
             PADO_CUDA(cudaFreeAsync(buf, s));
             PADO_CUDA(cudaStreamSynchronize(s));
         } catch (...) {
+            if (s2) cudaStreamSynchronize(s2);
+            cudaStreamSynchronize(s);
             cudaFreeAsync(buf, s);
             cudaStreamSynchronize(s);
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
             throw;
         }
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
     });
 }
 

@@ -202,6 +202,35 @@ def test_query_device_pointers(pado):
     assert np.array_equal(out.cpu().numpy(), idx.query(qa, qb))
 
 
+@pytest.mark.parametrize("weighted", [False, True])
+def test_chunked_host_query(pado, weighted):
+    """More pairs than one chunk of the host query path (2^21 pairs): the
+    chunks alternate between two streams and each chunk's results are read
+    back after the next chunk is queued.  Results equal one device launch over
+    all pairs and, on a sample, the oracle."""
+    import torch
+    k = (2 << 21) + 12345
+    if weighted:
+        g = G.rmat(10, 8, 18, weights=(1, 100))
+        idx, lab = gpu_w(pado, g, G.degree_rank(g), 128)
+    else:
+        g = G.rmat(10, 8, 18)
+        idx, lab = gpu_unw(pado, g, G.degree_rank(g), 16, 128)
+    qa, qb = G.random_pairs(g.n, k, 11, distinct=False)
+    qa[::100003] = g.n + 7  # out-of-range ids in several chunks
+    got = idx.query(qa, qb)
+    a = torch.from_numpy(qa.view(np.int32)).cuda()
+    b = torch.from_numpy(qb.view(np.int32)).cuda()
+    out = torch.empty(k, dtype=torch.int16 if weighted else torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    idx.query_device(a.data_ptr(), b.data_ptr(), out.data_ptr(), k, s.cuda_stream)
+    s.synchronize()
+    assert np.array_equal(got, out.cpu().numpy())
+    sel = np.r_[0:2000, (1 << 21) - 1000:(1 << 21) + 1000, k - 2000:k]
+    want = (orc.w_query if weighted else orc.unw_query)(lab, qa[sel], qb[sel])
+    assert np.array_equal(got[sel], want)
+
+
 @pytest.mark.parametrize("n", [1, 2, 5])
 def test_tiny_and_edgeless_graphs(pado, n):
     g = G.CSRGraph(n=n, off=np.zeros(n + 1, np.uint64), adj=np.zeros(0, np.uint32))
