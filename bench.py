@@ -414,7 +414,8 @@ def main():
     if qk in prof and prof[qk]["bytes"]:
         ach = prof[qk]["bytes"] / (prof[qk]["ms"] / 1e3) / 1e9
         q_roof = {"kernel": qk, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                  "bytes_per_launch": prof[qk]["bytes"] / prof[qk]["launches"]}
+                  "bytes_per_launch": prof[qk]["bytes"] / prof[qk]["launches"],
+                  "traffic": traffic_from_profiles(qk, args.workload) if nq == wl["queries"] else None}
 
     # ---- CPU baseline (bounded sample) ----
     cpu = None
