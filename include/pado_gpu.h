@@ -228,7 +228,9 @@ int pado_get_info(const pado_index *h, pado_info *info);
 
 /* Host buffers: off[n+1], hub[num_labels], dist[num_labels] (uint8 for
  * unweighted, int16 for weighted), bp_dist[n*bp_roots] and
- * bp_sets[n*bp_roots*2] (S^-1, S^0 per root; unweighted only, may be NULL). */
+ * bp_sets[n*bp_roots*2] (S^-1, S^0 per root; unweighted only, may be NULL).
+ * Page-locked buffers (cudaHostAlloc / cudaHostRegister) are written by the
+ * device directly; pageable ones are staged through device memory. */
 int pado_export(const pado_index *h, uint64_t *off, uint32_t *hub, void *dist, uint8_t *bp_dist,
                 uint64_t *bp_sets);
 

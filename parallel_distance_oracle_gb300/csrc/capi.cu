@@ -287,6 +287,20 @@ void build_ingested(pado_index *h, pado::IngestResult &r, uint32_t K, uint32_t B
     label_into(h, hg, g, h->K, B, s, phase);
 }
 
+// The device alias of page-locked host memory (cudaHostAlloc /
+// cudaHostRegister), which kernels may write directly; null for any other
+// pointer.
+void *mapped_host(void *p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // an unknown pointer is not an error here
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 // Export in original-id order: vertex v takes the list (and BP row) of rank[v].
 __global__ void __launch_bounds__(256) export_permute_kernel(uint32_t n, uint32_t K, int bp, const uint32_t *rank,
                                                              const uint64_t *roff, const uint64_t *noff,
@@ -919,22 +933,30 @@ int pado_export(const pado_index *h, uint64_t *off, uint32_t *hub, void *dist, u
         PADO_CUDA(cudaStreamSynchronize(s));
         off[0] = 0;
         for (uint32_t v = 0; v < n; ++v) off[v + 1] = off[v] + (roff[rk[v] + 1] - roff[rk[v]]);
+        // a page-locked destination is written by the gather kernel itself
+        // (through its device alias); any other goes through a device buffer
+        // and one copy
+        uint32_t *ohub = tot ? static_cast<uint32_t *>(mapped_host(hub)) : nullptr;
+        uint8_t *odist = tot ? static_cast<uint8_t *>(mapped_host(dist)) : nullptr;
+        uint8_t *obpd = bp && bp_dist ? static_cast<uint8_t *>(mapped_host(bp_dist)) : nullptr;
+        uint64_t *obps = bp && bp_sets ? static_cast<uint64_t *>(mapped_host(bp_sets)) : nullptr;
         pado::DBuf<uint64_t> noff(n + 1);
-        pado::DBuf<uint32_t> thub(std::max<uint64_t>(tot, 1));
-        pado::DBuf<uint8_t> tdist(std::max<uint64_t>(tot * dsz, 1));
-        pado::DBuf<uint8_t> tbpd(bp ? (uint64_t)n * K : 1);
-        pado::DBuf<uint64_t> tbps(bp ? (uint64_t)n * K * 2 : 1);
+        pado::DBuf<uint32_t> thub(ohub ? 1 : std::max<uint64_t>(tot, 1));
+        pado::DBuf<uint8_t> tdist(odist ? 1 : std::max<uint64_t>(tot * dsz, 1));
+        pado::DBuf<uint8_t> tbpd(bp && !obpd ? (uint64_t)n * K : 1);
+        pado::DBuf<uint64_t> tbps(bp && !obps ? (uint64_t)n * K * 2 : 1);
         noff.upload(off, n + 1, s);
         if (n)
             PADO_LAUNCH("export_permute_kernel", s,
                         export_permute_kernel<<<pado::grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(
                             n, K, bp ? 1 : 0, h->rank.p, h->store.off.p, noff.p, h->store.hub.p,
-                            static_cast<const uint8_t *>(ddist), (uint32_t)dsz, h->bpd.p, h->bps.p, thub.p, tdist.p,
-                            tbpd.p, tbps.p));
-        thub.download(hub, tot, s);
-        tdist.download(static_cast<uint8_t *>(dist), tot * dsz, s);
-        if (K && bp_dist) tbpd.download(bp_dist, (uint64_t)n * K, s);
-        if (K && bp_sets) tbps.download(bp_sets, (uint64_t)n * K * 2, s);
+                            static_cast<const uint8_t *>(ddist), (uint32_t)dsz, h->bpd.p, h->bps.p,
+                            ohub ? ohub : thub.p, odist ? odist : tdist.p, obpd ? obpd : tbpd.p,
+                            obps ? obps : tbps.p));
+        if (!ohub) thub.download(hub, tot, s);
+        if (!odist) tdist.download(static_cast<uint8_t *>(dist), tot * dsz, s);
+        if (K && bp_dist && !obpd) tbpd.download(bp_dist, (uint64_t)n * K, s);
+        if (K && bp_sets && !obps) tbps.download(bp_sets, (uint64_t)n * K * 2, s);
         PADO_CUDA(cudaStreamSynchronize(s));
     });
 }

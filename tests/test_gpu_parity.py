@@ -231,6 +231,47 @@ def test_chunked_host_query(pado, weighted):
     assert np.array_equal(got[sel], want)
 
 
+@pytest.mark.parametrize("weighted", [False, True])
+def test_export_into_page_locked_buffers(pado, weighted):
+    """pado_export writes page-locked destinations from its gather kernel and
+    stages pageable ones through device buffers; every mix gives the same
+    arrays as an export into pageable memory."""
+    import ctypes as C
+    import torch
+    from parallel_distance_oracle_gb300 import _lib
+    if weighted:
+        g = G.rmat(11, 8, 19, weights=(1, 100))
+        idx, lab = gpu_w(pado, g, G.degree_rank(g), 256)
+    else:
+        g = G.rmat(11, 8, 19)
+        idx, lab = gpu_unw(pado, g, G.degree_rank(g), 40, 256)
+    inf = idx.info()
+    n, K, tot = inf.n, inf.bp_roots, inf.num_labels
+    dt = np.int16 if weighted else np.uint8
+    want = [lab.off, lab.hub, lab.dist] + ([lab.bpd, lab.bps] if K else [])
+    shapes = [(n + 1, np.uint64), (tot, np.uint32), (tot, dt)] + ([(n * K, np.uint8), (n * K * 2, np.uint64)]
+                                                                  if K else [])
+    tdt = {np.uint64: torch.int64, np.uint32: torch.int32, np.uint8: torch.uint8, np.int16: torch.int16}
+    for pinned in ([True] * len(shapes), [i % 2 == 0 for i in range(len(shapes))],
+                   [i % 2 == 1 for i in range(len(shapes))]):
+        bufs, views = [], []
+        for (cnt, d), pin in zip(shapes, pinned):
+            if pin:
+                t = torch.zeros(max(cnt, 1), dtype=tdt[d]).pin_memory()
+                bufs.append(t)
+                views.append(t.numpy().view(d)[:cnt])
+            else:
+                a = np.zeros(max(cnt, 1), d)
+                bufs.append(a)
+                views.append(a[:cnt])
+        ptrs = [C.c_void_p(b.data_ptr() if isinstance(b, torch.Tensor) else b.ctypes.data) for b in bufs]
+        if not K:
+            ptrs += [None, None]
+        _lib.check(_lib.lib.pado_export(idx._h, *ptrs))
+        for got, exp in zip(views, want):
+            assert np.array_equal(got, np.asarray(exp).view(got.dtype)[:got.size]), pinned
+
+
 @pytest.mark.parametrize("n", [1, 2, 5])
 def test_tiny_and_edgeless_graphs(pado, n):
     g = G.CSRGraph(n=n, off=np.zeros(n + 1, np.uint64), adj=np.zeros(0, np.uint32))
