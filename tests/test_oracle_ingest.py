@@ -4,16 +4,14 @@ tests/golden/make_ingest_golden.py, and -- where the reference tree and the
 compiled reference driver are present -- the reference run directly on random
 edge lists and on the reference's own fixture files.  Dedupe is pinned to the
 benchmark generator's cleaning (graphs.csr_from_edges)."""
-from pathlib import Path
-
 import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from oracle import orc
+from oracle import build_oracle, orc
 from parallel_distance_oracle_gb300 import graphs as G
 
-REF_TOOLS = Path("/root/reference/tools")
+REF_TOOLS = build_oracle._reference_dir() / "tools"  # the reference's fixture files
 CASES = ["dups_unw", "dups_w", "rmat10_raw", "text_unw", "text_w", "text_unw_nolf"]
 
 
