@@ -322,6 +322,52 @@ __global__ void __launch_bounds__(256) export_permute_kernel(uint32_t n, uint32_
     }
 }
 
+// One graph's share of the union label store, BP rows and ranks, and the
+// graph's own buffers they are copied into.
+struct SplitDesc {
+    uint64_t l0, tot;   // its labels: union entries [l0, l0 + tot)
+    uint32_t base, ng;  // its vertices: union ids [base, base + ng)
+    uint64_t *off;      // ng + 1 offsets, rebased to l0
+    uint32_t *hub;
+    uint8_t *dist8;
+    uint8_t *bpd;       // ng * K
+    uint64_t *bps;      // ng * K * 2
+    uint32_t *rank;     // ng entries, or null
+};
+
+// The union's label offsets at the graph boundaries: bnd[i] = aoff[gbase[i]].
+__global__ void split_bounds_kernel(const uint64_t *__restrict__ aoff, const uint32_t *__restrict__ gbase,
+                                    uint32_t G, uint64_t *__restrict__ bnd)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= G) bnd[i] = aoff[gbase[i]];
+}
+
+// All graphs' copies in one launch: the blocks of grid row y copy graph y's
+// slices, striding over its elements together.
+__global__ void __launch_bounds__(256) split_many_kernel(const SplitDesc *__restrict__ ds, uint32_t K,
+                                                         const uint64_t *__restrict__ aoff,
+                                                         const uint32_t *__restrict__ ahub,
+                                                         const uint8_t *__restrict__ adist,
+                                                         const uint8_t *__restrict__ abpd,
+                                                         const uint64_t *__restrict__ abps,
+                                                         const uint32_t *__restrict__ arank)
+{
+    const SplitDesc d = ds[blockIdx.y];
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t st = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = t; i <= d.ng; i += st) d.off[i] = aoff[d.base + i] - d.l0;
+    for (uint64_t i = t; i < d.tot; i += st) {
+        d.hub[i] = ahub[d.l0 + i];
+        d.dist8[i] = adist[d.l0 + i];
+    }
+    const uint64_t nb = (uint64_t)d.ng * K, b0 = (uint64_t)d.base * K;
+    for (uint64_t i = t; i < nb; i += st) d.bpd[i] = abpd[b0 + i];
+    for (uint64_t i = t; i < 2 * nb; i += st) d.bps[i] = abps[2 * b0 + i];
+    if (d.rank)
+        for (uint64_t i = t; i < d.ng; i += st) d.rank[i] = arank[d.base + i];
+}
+
 // Many graphs laid side by side: graph i relabeled by its rank and shifted to
 // ids [gbase[i], gbase[i+1]).
 struct UnionGraph {
@@ -774,46 +820,50 @@ int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *of
         pado::LabelStore all;
         pado::LabelRun run = pado::unw_label_many(r.g, u.gbase, bp_roots, batch, r.used, r.bpd.p, r.bps.p, all, s);
         phase("labeling");
+        // split: label totals at the graph boundaries, one upload of every
+        // graph's ranks, then per graph its buffers, and ONE kernel copies
+        // every graph's slices (offsets rebased on the device)
         const uint32_t N = u.hg.n;
-        std::vector<uint64_t> fo(N + 1);
-        all.off.download(fo.data(), N + 1, s);
-        PADO_CUDA(cudaStreamSynchronize(s));
         const uint32_t K = bp_roots;
-        // every graph's offsets, rebased to its own list start, in one host
-        // array that outlives the uploads (one synchronisation at the end)
-        std::vector<uint64_t> lo_all((uint64_t)N + G);
+        std::vector<uint64_t> bnd(G + 1);
+        {
+            pado::DBuf<uint32_t> dgb(G + 1);
+            pado::DBuf<uint64_t> dbnd(G + 1);
+            dgb.upload(u.gbase.data(), G + 1, s);
+            PADO_LAUNCH("split_bounds_kernel", s,
+                        split_bounds_kernel<<<(G + 256) / 256, 256, 0, s>>>(all.off.p, dgb.p, G, dbnd.p));
+            dbnd.download(bnd.data(), G + 1, s);
+            PADO_CUDA(cudaStreamSynchronize(s));
+        }
+        std::vector<uint32_t> rank_all;
+        pado::DBuf<uint32_t> drank;
+        if (rank) {
+            rank_all.assign(std::max<uint32_t>(N, 1), 0);
+            for (uint32_t i = 0; i < G; ++i)
+                if (rank[i] && n[i]) memcpy(rank_all.data() + u.gbase[i], rank[i], (size_t)n[i] * 4);
+            drank.alloc_async(rank_all.size(), s);
+            drank.upload(rank_all.data(), rank_all.size(), s);
+        }
+        std::vector<SplitDesc> desc(G);
         for (uint32_t i = 0; i < G; ++i) {
             const uint32_t base = u.gbase[i], ng = n[i];
+            const uint64_t l0 = bnd[i], tot = bnd[i + 1] - l0;
             std::unique_ptr<pado_index> h(new pado_index);
             h->device = dev;
             h->kind = PADO_UNWEIGHTED;
             h->n = ng;
             h->K = K;
             h->B = batch;
-            if (rank && rank[i]) {
-                h->rank.alloc_async(std::max<uint32_t>(ng, 1), s);
-                h->rank.upload(rank[i], ng, s);
-            }
-            const uint64_t l0 = fo[base], tot = fo[base + ng] - l0;
-            uint64_t *lo = lo_all.data() + base + i;  // ng + 1 entries
-            for (uint32_t v = 0; v <= ng; ++v) lo[v] = fo[base + v] - l0;
+            const bool ranked = rank && rank[i];
+            if (ranked) h->rank.alloc_async(std::max<uint32_t>(ng, 1), s);
             h->store.total = tot;
             h->store.off.alloc_async(ng + 1, s);
-            h->store.off.upload(lo, ng + 1, s);
             h->store.hub.alloc_async(std::max<uint64_t>(tot, 1), s);
             h->store.dist8.alloc_async(std::max<uint64_t>(tot, 1), s);
-            if (tot) {
-                PADO_CUDA(cudaMemcpyAsync(h->store.hub.p, all.hub.p + l0, tot * 4, cudaMemcpyDeviceToDevice, s));
-                PADO_CUDA(cudaMemcpyAsync(h->store.dist8.p, all.dist8.p + l0, tot, cudaMemcpyDeviceToDevice, s));
-            }
             h->bpd.alloc_async(std::max<uint64_t>((uint64_t)ng * K, 1), s);
             h->bps.alloc_async(std::max<uint64_t>((uint64_t)ng * K * 2, 1), s);
-            if ((uint64_t)ng * K) {
-                PADO_CUDA(cudaMemcpyAsync(h->bpd.p, r.bpd.p + (uint64_t)base * K, (uint64_t)ng * K,
-                                          cudaMemcpyDeviceToDevice, s));
-                PADO_CUDA(cudaMemcpyAsync(h->bps.p, r.bps.p + (uint64_t)base * K * 2, (uint64_t)ng * K * 16,
-                                          cudaMemcpyDeviceToDevice, s));
-            }
+            desc[i] = SplitDesc{l0, tot, base, ng, h->store.off.p, h->store.hub.p, h->store.dist8.p, h->bpd.p,
+                                h->bps.p, ranked ? h->rank.p : nullptr};
             h->info.n = ng;
             h->info.kind = PADO_UNWEIGHTED;
             h->info.bp_roots = K;
@@ -826,7 +876,13 @@ int pado_unw_build_many(uint32_t G, const uint32_t *n, const uint64_t *const *of
             h->info.device_bytes = h->device_bytes();
             hs[i] = std::move(h);
         }
-        PADO_CUDA(cudaStreamSynchronize(s));  // lo_all and the copies
+        pado::DBuf<SplitDesc> ddesc;
+        ddesc.alloc_async(G, s);
+        ddesc.upload(desc.data(), G, s);
+        PADO_LAUNCH("split_many_kernel", s,
+                    split_many_kernel<<<dim3(16, G), 256, 0, s>>>(ddesc.p, K, all.off.p, all.hub.p, all.dist8.p,
+                                                                 r.bpd.p, r.bps.p, rank ? drank.p : nullptr));
+        PADO_CUDA(cudaStreamSynchronize(s));  // rank_all, desc and the copies
         phase("split");
     });
     if (st == PADO_OK)
