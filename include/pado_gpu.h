@@ -168,6 +168,43 @@ int pado_graph_ingest_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_
                              uint32_t flags, uint64_t *d_off, uint32_t *d_adj, uint8_t *d_w_out, uint32_t *d_rank,
                              uint64_t *entries, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Graph reductions: the reference's two graph-conversion tools on the device.
+ * Both take an edge list (u[i], v[i]) in input order over ids < n (the tools
+ * use n = max id + 1), build the tools' adjacency (both directions of every
+ * input edge; repeats and self-loops stay and count), and return per-vertex
+ * flags plus the indices of the input edges that survive, in input order --
+ * the edges the tools write.  m < 2^31 edges, n < 2^31 vertices.
+ * ------------------------------------------------------------------------- */
+
+/* Replaces tools/pseudocode-delete_1-degree_vertices.cpp
+ * (Graph::delete_1_degree_vertices, :127-199): every vertex with one
+ * adjacency entry is deleted together with the chain of two-entry vertices
+ * behind it, up to but not including the first vertex whose entry count is
+ * not 2 (a path component goes entirely).  deleted[n]: 1 = deleted;
+ * kept[*m_kept] (room for m): indices of the edges with no deleted end. */
+int pado_reduce_degree1(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint8_t *deleted,
+                        uint64_t *kept, uint64_t *m_kept);
+
+/* Replaces distributed_version/tools/graph-convert/remove_equivalent_vertices.cpp
+ * (eliminate_vertices, :96-338): vertices whose sets {x} + adjacency entries
+ * are equal multisets form a class; the smallest id of a class stays and the
+ * others get redundant[x] = 1.  new_id[n] numbers the vertices that stay in
+ * ascending id (2^32 - 1 for redundant ones); kept as above; *n_out = 1 + the
+ * largest new id on a kept edge (0 if none), the vertex count the tool
+ * writes before its (new_id[u], new_id[v]) pairs. */
+int pado_reduce_equivalent(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint8_t *redundant,
+                           uint32_t *new_id, uint64_t *kept, uint64_t *m_kept, uint32_t *n_out);
+
+/* Same with every array in device memory (the current device), on `stream`
+ * (a cudaStream_t; NULL: the legacy default stream); they return when the
+ * outputs are written.  d_kept needs room for m entries. */
+int pado_reduce_degree1_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t n, uint8_t *d_deleted,
+                               uint64_t *d_kept, uint64_t *m_kept, void *stream);
+int pado_reduce_equivalent_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t n,
+                                  uint8_t *d_redundant, uint32_t *d_new_id, uint64_t *d_kept, uint64_t *m_kept,
+                                  uint32_t *n_out, void *stream);
+
 /* The ingest calls take their scratch (sort keys and buffers, about 24
  * bytes per edge) from a memory pool of the library's own, in stream order.
  * Up to `bytes` of it stay reserved on the current device between calls

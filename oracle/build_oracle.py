@@ -21,6 +21,14 @@ Two products, both git-ignored build outputs:
   Staging needs the reference tree (``PADO_REFERENCE_DIR``, default: the
   mounted reference); compiling only needs the staged copy, so a host that
   received ``oracle/_ref/inc`` can build the driver without the tree.
+* ``oracle/_ref/delete_1_degree`` and ``oracle/_ref/remove_equivalent`` -- the
+  reference's two graph-conversion tools (``tools/pseudocode-delete_1-degree_
+  vertices.cpp``, ``distributed_version/tools/graph-convert/
+  remove_equivalent_vertices.cpp``) compiled unchanged where they lie in the
+  reference tree; their headers miss ``<cstdint>`` (and the first ``<cstdio>``/
+  ``<cstdlib>``), which the compiler's ``-include`` supplies.  Built only where
+  the tree is present: they make the graph-reduction fixtures and pin the
+  oracle's reductions in the CPU tests.
 """
 from __future__ import annotations
 
@@ -130,9 +138,40 @@ def build_reference(force: bool = False, sizes=REF_BP_SIZES) -> list[Path]:
     return outs
 
 
+REF_TOOLS = {
+    "delete_1_degree": ("tools/pseudocode-delete_1-degree_vertices.cpp", [], []),
+    "remove_equivalent": ("distributed_version/tools/graph-convert/remove_equivalent_vertices.cpp",
+                          ["distributed_version/includes", "includes"], ["-fopenmp"]),
+}
+
+
+def ref_tool(name: str) -> Path:
+    return REF_OUT / name
+
+
+def build_reference_tools(force: bool = False) -> list[Path]:
+    """Compile the reference's graph-conversion tools.  [] without the tree."""
+    root = _reference_dir()
+    outs = []
+    for name, (src, incs, extra) in REF_TOOLS.items():
+        path = root / src
+        if not path.exists():
+            return []
+        out = ref_tool(name)
+        outs.append(out)
+        if not force and _newer(out, path):
+            continue
+        REF_OUT.mkdir(parents=True, exist_ok=True)
+        cmd = (["g++", "-std=c++14", "-O2", "-w", "-include", "cstdint", "-include", "cstdio", "-include", "cstdlib"]
+               + extra + sum((["-I", str(root / i)] for i in incs), []) + [str(path), "-o", str(out)])
+        subprocess.run(cmd, check=True)
+    return outs
+
+
 def build_all() -> None:
     build_port()
     build_reference()
+    build_reference_tools()
 
 
 if __name__ == "__main__":

@@ -90,6 +90,12 @@ def port() -> C.CDLL:
         lib.orc_edge_text_parse.restype = C.c_uint64
         lib.orc_edge_text_parse.argtypes = [C.c_char_p, C.c_uint64, C.c_int, C.c_uint64, C.c_void_p, C.c_void_p,
                                             C.c_void_p]
+        lib.orc_reduce_degree1.restype = C.c_int
+        lib.orc_reduce_degree1.argtypes = [C.c_uint64, _u32p, _u32p, C.c_uint32, _u8p, _u64p,
+                                           C.POINTER(C.c_uint64), C.POINTER(C.c_int)]
+        lib.orc_reduce_equivalent.restype = C.c_int
+        lib.orc_reduce_equivalent.argtypes = [C.c_uint64, _u32p, _u32p, C.c_uint32, _u8p, _u32p, _u64p,
+                                              C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]
         _port = lib
     return _port
 
@@ -378,3 +384,83 @@ def unw_prefix_sample(g, rank, K: int, B: int, nbatches: int, threads: int = 0):
         secs = port().orc_unw_prefix(*args, K, B, nbatches, C.byref(labels), C.byref(bp))
         kind, cores = "port", 1
     return {"seconds": secs, "labels": int(labels.value), "bp_seconds": bp.value, "kind": kind, "cores": cores}
+
+
+# ---- graph reductions --------------------------------------------------------
+
+def _edges_n(u, v, n):
+    u, v = _c(u, np.uint32), _c(v, np.uint32)
+    if n == 0 and len(u):
+        n = int(max(u.max(), v.max())) + 1
+    return u, v, n
+
+
+def reduce_degree1(u, v, n: int = 0):
+    """orc_reduce_degree1 (the reference's degree-1 chain deletion).  n = 0
+    takes max id + 1.  Returns (deleted uint8[n], kept edge indices,
+    nonterminating)."""
+    u, v, n = _edges_n(u, v, n)
+    m = len(u)
+    deleted = np.zeros(max(n, 1), np.uint8)
+    kept = np.zeros(max(m, 1), np.uint64)
+    k, nt = C.c_uint64(), C.c_int()
+    if port().orc_reduce_degree1(m, u, v, n, deleted, kept, C.byref(k), C.byref(nt)) != 0:
+        raise ValueError("edge endpoint out of range")
+    return deleted[:n], kept[:k.value].copy(), bool(nt.value)
+
+
+def reduce_equivalent(u, v, n: int = 0):
+    """orc_reduce_equivalent (the reference's equivalent-vertex removal).
+    Returns (redundant uint8[n], new_id uint32[n], kept edge indices, n_out)."""
+    u, v, n = _edges_n(u, v, n)
+    m = len(u)
+    red = np.zeros(max(n, 1), np.uint8)
+    nid = np.zeros(max(n, 1), np.uint32)
+    kept = np.zeros(max(m, 1), np.uint64)
+    k, nout = C.c_uint64(), C.c_uint32()
+    if port().orc_reduce_equivalent(m, u, v, n, red, nid, kept, C.byref(k), C.byref(nout)) != 0:
+        raise ValueError("edge endpoint out of range")
+    return red[:n], nid[:n], kept[:k.value].copy(), int(nout.value)
+
+
+def ref_tools_available() -> bool:
+    from oracle import build_oracle
+    return all(build_oracle.ref_tool(t).exists() for t in build_oracle.REF_TOOLS)
+
+
+def _write_edges(path, u, v):
+    with open(path, "w") as f:
+        f.write("".join(f"{a} {b}\n" for a, b in zip(u.tolist(), v.tolist())))
+
+
+def ref_delete_degree1(u, v, timeout: float = 60.0) -> np.ndarray:
+    """The reference's delete_1-degree tool on the edge list: its output
+    edges, shape (k, 2), in the order it writes them."""
+    import subprocess
+    import tempfile
+    from oracle import build_oracle
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = f"{d}/in.txt", f"{d}/out.txt"
+        _write_edges(fin, _c(u, np.uint32), _c(v, np.uint32))
+        subprocess.run([str(build_oracle.ref_tool("delete_1_degree")), fin, fout], check=True, timeout=timeout,
+                       stdout=subprocess.DEVNULL)
+        rows = [ln.split() for ln in open(fout).read().splitlines() if ln.strip()]
+    return np.array(rows, np.uint32).reshape(-1, 2)
+
+
+def ref_remove_equivalent(u, v, timeout: float = 60.0):
+    """The reference's remove_equivalent_vertices tool: (num_v, edges (k, 2))
+    read from the binary file it writes."""
+    import subprocess
+    import tempfile
+    from oracle import build_oracle
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout, flog = f"{d}/in.txt", f"{d}/out.bin", f"{d}/log.txt"
+        _write_edges(fin, _c(u, np.uint32), _c(v, np.uint32))
+        open(flog, "w").close()
+        subprocess.run([str(build_oracle.ref_tool("remove_equivalent")), fin, fout, flog], check=True,
+                       timeout=timeout, stdout=subprocess.DEVNULL, env={"OMP_NUM_THREADS": "1"})
+        b = open(fout, "rb").read()
+    nv = int(np.frombuffer(b[:4], np.uint32)[0])
+    ne = int(np.frombuffer(b[4:12], np.uint64)[0])
+    return nv, np.frombuffer(b[12:12 + 8 * ne], np.uint32).reshape(-1, 2).copy()

@@ -27,6 +27,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <map>
 #include <queue>
 #include <utility>
 #include <vector>
@@ -1092,6 +1093,105 @@ uint64_t orc_edge_text_parse(const char *text, uint64_t bytes, int weighted, uin
         start = end + 1;
     }
     return count;
+}
+
+// ---- graph reductions (the reference's conversion tools) --------------------
+//
+// Both take the edge list in input order over ids < n and keep every input
+// edge's two adjacency entries (repeats and self-loops included), as the tools
+// build their adjacency; both return per-vertex flags and the indices of the
+// input edges that survive, in input order -- the lines the tools write.
+
+// tools/pseudocode-delete_1-degree_vertices.cpp: adjacency in input order
+// (construct :101-124; a self-loop is two entries of its vertex), degrees of
+// the input graph throughout (:130, :153); for every vertex in ascending id
+// that is not deleted and has one entry, a walk (:131-166) deletes the current
+// vertex, takes its first entry that is not deleted (the last entry if all
+// are), and continues there if that vertex has two entries.  Kept edges have
+// no deleted end (:185-191).  The reference's walk can bounce for ever between
+// deleted vertices of two entries (e.g. the path 0-2-3-1 given as the lines
+// "0 2", "3 1", "2 3", whose end 1 walks 1 -> 3 -> 2 -> 3 -> ...); after
+// n + 1 steps without a new deletion the restatement ends such a walk and sets
+// *nonterminating (no deletion can happen in it any more).
+int orc_reduce_degree1(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint8_t *deleted,
+                       uint64_t *kept, uint64_t *m_kept, int *nonterminating)
+{
+    for (uint64_t e = 0; e < m; ++e)
+        if (u[e] >= n || v[e] >= n) return 1;
+    std::vector<std::vector<uint32_t>> adj(n);
+    for (uint64_t e = 0; e < m; ++e) {
+        adj[u[e]].push_back(v[e]);
+        adj[v[e]].push_back(u[e]);
+    }
+    const uint32_t NONE = 0xffffffffu;
+    std::fill(deleted, deleted + n, (uint8_t)0);
+    *nonterminating = 0;
+    for (uint32_t s = 0; s < n; ++s) {
+        uint32_t next = (!deleted[s] && adj[s].size() == 1) ? s : NONE;
+        uint64_t idle = 0;  // steps since the last new deletion
+        while (next != NONE) {
+            const uint32_t x = next;
+            if (deleted[x]) {
+                if (++idle > (uint64_t)n + 1) {
+                    *nonterminating = 1;
+                    break;
+                }
+            } else {
+                idle = 0;
+            }
+            deleted[x] = 1;
+            uint32_t w = NONE;
+            for (uint32_t y : adj[x]) {
+                w = y;
+                if (!deleted[y]) break;
+            }
+            next = (w != NONE && adj[w].size() == 2) ? w : NONE;
+        }
+    }
+    uint64_t k = 0;
+    for (uint64_t e = 0; e < m; ++e)
+        if (!deleted[u[e]] && !deleted[v[e]]) kept[k++] = e;
+    *m_kept = k;
+    return 0;
+}
+
+// distributed_version/tools/graph-convert/remove_equivalent_vertices.cpp:
+// vertex x's set is {x} plus its adjacency entries, sorted (:151-167, a
+// multiset); vertices are taken by (set size, id) (:168-181) and within one
+// size every vertex that is not yet redundant marks each later vertex with an
+// equal set redundant (:230-287).  Set equality is an equivalence, so that
+// leaves exactly the smallest id of every class of equal sets; the
+// restatement finds the classes with an ordered map instead of comparing
+// pairs within a size.  The rest are numbered by ascending id (:295-303) and
+// the kept edges (no redundant end, :318-327) written with those ids; the
+// tool's vertex count is 1 + the largest new id on a kept edge (:322), 0 when
+// no edge is kept.  new_id of a redundant vertex is 2^32 - 1.
+int orc_reduce_equivalent(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint8_t *redundant,
+                          uint32_t *new_id, uint64_t *kept, uint64_t *m_kept, uint32_t *n_out)
+{
+    for (uint64_t e = 0; e < m; ++e)
+        if (u[e] >= n || v[e] >= n) return 1;
+    std::vector<std::vector<uint32_t>> set(n);
+    for (uint32_t x = 0; x < n; ++x) set[x].push_back(x);
+    for (uint64_t e = 0; e < m; ++e) {
+        set[u[e]].push_back(v[e]);
+        set[v[e]].push_back(u[e]);
+    }
+    for (auto &l : set) std::sort(l.begin(), l.end());
+    std::map<std::vector<uint32_t>, uint32_t> first;
+    for (uint32_t x = 0; x < n; ++x) redundant[x] = first.emplace(set[x], x).second ? 0 : 1;
+    uint32_t next = 0;
+    for (uint32_t x = 0; x < n; ++x) new_id[x] = redundant[x] ? 0xffffffffu : next++;
+    uint64_t k = 0;
+    uint32_t top = 0;
+    for (uint64_t e = 0; e < m; ++e)
+        if (!redundant[u[e]] && !redundant[v[e]]) {
+            kept[k++] = e;
+            top = std::max(top, std::max(new_id[u[e]], new_id[v[e]]) + 1);
+        }
+    *m_kept = k;
+    *n_out = top;
+    return 0;
 }
 
 }  // extern "C"

@@ -61,6 +61,10 @@ def _load() -> C.CDLL:
         "pado_graph_ingest": (C.c_int, [u64, vp, vp, vp, u32, u32, vp, vp, vp, vp, P(u64)]),
         "pado_graph_ingest_device": (C.c_int, [u64, vp, vp, vp, u32, u32, vp, vp, vp, vp, P(u64), vp]),
         "pado_set_scratch_cache": (C.c_int, [u64]),
+        "pado_reduce_degree1": (C.c_int, [u64, vp, vp, u32, vp, vp, P(u64)]),
+        "pado_reduce_equivalent": (C.c_int, [u64, vp, vp, u32, vp, vp, vp, P(u64), P(u32)]),
+        "pado_reduce_degree1_device": (C.c_int, [u64, vp, vp, u32, vp, vp, P(u64), vp]),
+        "pado_reduce_equivalent_device": (C.c_int, [u64, vp, vp, u32, vp, vp, vp, P(u64), P(u32), vp]),
         "pado_unw_build_edges": (C.c_int, [u64, vp, vp, u32, u32, u32, u32, P(vp)]),
         "pado_w_build_edges": (C.c_int, [u64, vp, vp, vp, u32, u32, u32, P(vp)]),
         "pado_build_edge_file": (C.c_int, [C.c_char_p, u32, u32, u32, u32, P(vp)]),
@@ -100,7 +104,8 @@ EXPORTED = [
     "pado_last_error", "pado_status_string", "pado_version", "pado_unw_build", "pado_unw_build_ranked",
     "pado_unw_build_many", "pado_unw_tune_batch",
     "pado_w_build", "pado_w_build_ranked", "pado_graph_ingest", "pado_graph_ingest_device",
-    "pado_set_scratch_cache",
+    "pado_set_scratch_cache", "pado_reduce_degree1", "pado_reduce_equivalent", "pado_reduce_degree1_device",
+    "pado_reduce_equivalent_device",
     "pado_unw_build_edges", "pado_w_build_edges",
     "pado_build_edge_file", "pado_edge_text_parse", "pado_set_order", "pado_free", "pado_get_info", "pado_export",
     "pado_import", "pado_query", "pado_query_device", "pado_query_noalloc", "pado_store", "pado_load",

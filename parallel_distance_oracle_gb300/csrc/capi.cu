@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -691,6 +692,91 @@ int pado_graph_ingest_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_
         pado::release_scratch(scratch_keep());
         *entries = r.m;
     });
+}
+
+int pado_reduce_degree1_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t n, uint8_t *d_deleted,
+                               uint64_t *d_kept, uint64_t *m_kept, void *stream)
+{
+    return guarded([&] {
+        PADO_CHECK(m == 0 || (d_u && d_v && d_kept), PADO_E_ARG, "null edge array");
+        PADO_CHECK(m_kept && (n == 0 || d_deleted), PADO_E_ARG, "null output");
+        const cudaStream_t s = (cudaStream_t)stream;
+        const pado::ReduceResult r = pado::reduce_degree1(m, d_u, d_v, n, s, d_deleted, d_kept);
+        pado::release_scratch(scratch_keep());
+        *m_kept = r.kept;
+    });
+}
+
+int pado_reduce_equivalent_device(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t n,
+                                  uint8_t *d_redundant, uint32_t *d_new_id, uint64_t *d_kept, uint64_t *m_kept,
+                                  uint32_t *n_out, void *stream)
+{
+    return guarded([&] {
+        PADO_CHECK(m == 0 || (d_u && d_v && d_kept), PADO_E_ARG, "null edge array");
+        PADO_CHECK(m_kept && n_out && (n == 0 || (d_redundant && d_new_id)), PADO_E_ARG, "null output");
+        const cudaStream_t s = (cudaStream_t)stream;
+        const pado::ReduceResult r = pado::reduce_equivalent(m, d_u, d_v, n, s, d_redundant, d_new_id, d_kept);
+        pado::release_scratch(scratch_keep());
+        *m_kept = r.kept;
+        *n_out = r.n_out;
+    });
+}
+
+namespace {
+
+// Host arrays in and out around a device reduction: the edges go up, flags,
+// new ids and kept indices come back.
+using ReduceRun = std::function<pado::ReduceResult(const uint32_t *, const uint32_t *, uint8_t *, uint32_t *,
+                                                     uint64_t *, cudaStream_t)>;
+
+int reduce_host(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint8_t *flags, uint32_t *new_id,
+                uint64_t *kept, uint64_t *m_kept, const ReduceRun &run)
+{
+    return guarded([&] {
+        PADO_CHECK(m == 0 || (u && v && kept), PADO_E_ARG, "null edge array");
+        PADO_CHECK(m_kept && (n == 0 || flags), PADO_E_ARG, "null output");
+        PADO_CHECK(m < (1ull << 31), PADO_E_ARG, "at most 2^31 - 1 edges");
+        StreamGuard sg;
+        const cudaStream_t s = sg.s;
+        pado::DBuf<uint32_t> du(std::max<uint64_t>(m, 1)), dv(std::max<uint64_t>(m, 1));
+        pado::DBuf<uint8_t> dflag(std::max<uint32_t>(n, 1));
+        pado::DBuf<uint32_t> dnid(new_id ? std::max<uint32_t>(n, 1) : 1);
+        pado::DBuf<uint64_t> dkept(std::max<uint64_t>(m, 1));
+        du.upload(u, m, s);
+        dv.upload(v, m, s);
+        const pado::ReduceResult r = run(du.p, dv.p, dflag.p, dnid.p, dkept.p, s);
+        dflag.download(flags, n, s);
+        if (new_id) dnid.download(new_id, n, s);
+        dkept.download(kept, r.kept, s);
+        PADO_CUDA(cudaStreamSynchronize(s));
+        pado::release_scratch(scratch_keep());
+        *m_kept = r.kept;
+    });
+}
+
+}  // namespace
+
+int pado_reduce_degree1(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint8_t *deleted,
+                        uint64_t *kept, uint64_t *m_kept)
+{
+    return reduce_host(m, u, v, n, deleted, nullptr, kept, m_kept,
+                       [&](const uint32_t *du, const uint32_t *dv, uint8_t *dflag, uint32_t *, uint64_t *dkept,
+                           cudaStream_t s) { return pado::reduce_degree1(m, du, dv, n, s, dflag, dkept); });
+}
+
+int pado_reduce_equivalent(uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t n, uint8_t *redundant,
+                           uint32_t *new_id, uint64_t *kept, uint64_t *m_kept, uint32_t *n_out)
+{
+    if (!n_out || (n && !new_id)) return fail(PADO_E_ARG, "null output");
+    pado::ReduceResult res;
+    const int st = reduce_host(m, u, v, n, redundant, new_id, kept, m_kept,
+                               [&](const uint32_t *du, const uint32_t *dv, uint8_t *dflag, uint32_t *dnid,
+                                   uint64_t *dkept, cudaStream_t s) {
+                                   res = pado::reduce_equivalent(m, du, dv, n, s, dflag, dnid, dkept);
+                                   return res;
+                               });
+    if (st == PADO_OK) *n_out = res.n_out;
+    return st;
 }
 
 namespace {

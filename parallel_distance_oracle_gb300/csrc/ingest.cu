@@ -645,6 +645,200 @@ __global__ void __launch_bounds__(256) edge_compact_kernel(const uint32_t *lu, c
     }
 }
 
+// ---- graph reductions (the reference's conversion tools) -------------------
+
+// For vertices with at most two adjacency entries, the entries themselves
+// (any order): nb[2x], nb[2x + 1].  Ids were range-checked by degree_kernel.
+__global__ void __launch_bounds__(256) red_small_adj_kernel(const uint32_t *u, const uint32_t *v, uint64_t m,
+                                                            const uint32_t *deg, uint32_t *fill, uint32_t *nb)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = u[e], b = v[e];
+        if (deg[a] <= 2) nb[2ull * a + atomicAdd(&fill[a], 1u)] = b;
+        if (deg[b] <= 2) nb[2ull * b + atomicAdd(&fill[b], 1u)] = a;
+    }
+}
+
+// Every vertex with one entry deletes itself and the chain of two-entry
+// vertices behind it, stopping before the first vertex whose entry count is
+// not 2.  Two walks meet only on a path component (both ends have one
+// entry); their marks are the same idempotent stores, so the flags do not
+// depend on the order the walks run in.  A chain cannot close on itself (its
+// vertices have two entries each); the step bound only guards that.
+__global__ void __launch_bounds__(256) red_walk_kernel(uint32_t n, const uint32_t *deg, const uint32_t *nb,
+                                                       uint8_t *del, uint32_t *status)
+{
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        if (deg[x] != 1) continue;
+        del[x] = 1;
+        uint32_t prev = x, cur = nb[2ull * x];
+        for (uint32_t steps = 0; deg[cur] == 2; ++steps) {
+            if (steps >= n) {
+                atomicOr(status, 1u);
+                break;
+            }
+            del[cur] = 1;
+            const uint32_t a = nb[2ull * cur], b = nb[2ull * cur + 1];
+            const uint32_t nx = a != prev ? a : b;
+            if (nx == prev) break;  // both entries lead back: nothing further on
+            prev = cur;
+            cur = nx;
+        }
+    }
+}
+
+// flag[e] = 1 when edge e has no dropped end (flag[m] stays 0 for the scan).
+__global__ void __launch_bounds__(256) red_keep_flag_kernel(const uint32_t *u, const uint32_t *v, uint64_t m,
+                                                            const uint8_t *drop, uint32_t *flag)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x)
+        flag[e] = (!drop[u[e]] && !drop[v[e]]) ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(256) red_keep_scatter_kernel(const uint32_t *pos, uint64_t m, uint64_t *kept)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x)
+        if (pos[e + 1] != pos[e]) kept[pos[e]] = e;
+}
+
+// Both adjacency entries of every edge as (src << bits | dst) keys.
+__global__ void __launch_bounds__(256) red_entry_key_kernel(const uint32_t *u, const uint32_t *v, uint64_t m,
+                                                            uint32_t bits, uint64_t *keys)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = u[e], b = v[e];
+        keys[2 * e] = a << bits | b;
+        keys[2 * e + 1] = b << bits | a;
+    }
+}
+
+__global__ void __launch_bounds__(256) red_extract_kernel(const uint64_t *keys, uint64_t L, uint64_t mask,
+                                                          uint32_t *adj)
+{
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < L; k += (uint64_t)gridDim.x * blockDim.x)
+        adj[k] = (uint32_t)(keys[k] & mask);
+}
+
+// SplitMix64's output function (Steele, Lea and Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014): a bijective 64-bit mixer.
+__device__ __forceinline__ uint64_t mix64(uint64_t x)
+{
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+// A warp per vertex x: a hash of the multiset {x} + its entries (a sum of
+// mixed elements does not depend on their order), folded with the set size
+// into 32 bits, as the key (hash << 32 | x).  Equal sets have equal upper
+// halves; the converse is checked exactly afterwards.
+__global__ void __launch_bounds__(256) red_hash_kernel(uint32_t n, const uint32_t *off, const uint32_t *adj,
+                                                       uint64_t *keys)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < n; x += nw) {
+        const uint32_t b = off[x], e = off[x + 1];
+        uint64_t h = 0;
+        for (uint32_t k = b + lane; k < e; k += 32) h += mix64(adj[k]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(FULLW, h, o);
+        if (lane == 0) {
+            h += mix64(x);
+            const uint64_t f = mix64(h ^ ((uint64_t)(e - b + 1) << 40));
+            keys[x] = (f >> 32) << 32 | x;
+        }
+    }
+}
+
+// Element k of x's sorted set: its sorted entries A[0, d) with x inserted at
+// position px (the count of entries below x).
+__device__ __forceinline__ uint32_t set_elem(const uint32_t *A, uint32_t px, uint32_t x, uint32_t k)
+{
+    return k < px ? A[k] : (k == px ? x : A[k - 1]);
+}
+
+// Whether x and y have equal sets (every lane returns it).
+__device__ bool same_set(uint32_t x, uint32_t y, const uint32_t *off, const uint32_t *adj, int lane)
+{
+    const uint32_t d = off[x + 1] - off[x];
+    if (off[y + 1] - off[y] != d) return false;
+    const uint32_t *A = adj + off[x], *B = adj + off[y];
+    uint32_t px = 0, py = 0;
+    for (uint32_t k = lane; k < d; k += 32) {
+        px += A[k] < x ? 1u : 0u;
+        py += B[k] < y ? 1u : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        px += __shfl_xor_sync(FULLW, px, o);
+        py += __shfl_xor_sync(FULLW, py, o);
+    }
+    for (uint32_t k0 = 0; k0 <= d; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        const bool diff = k <= d && set_elem(A, px, x, k) != set_elem(B, py, y, k);
+        if (__any_sync(FULLW, diff)) return false;
+    }
+    return true;
+}
+
+// A warp per position p of the (hash, id)-sorted keys: a vertex that is not
+// the first of its hash run compares its set with the run's earlier vertices
+// in ascending id and is redundant at the first equal one -- so exactly the
+// smallest id of every class of equal sets stays.
+__global__ void __launch_bounds__(256) red_twin_kernel(uint32_t n, const uint64_t *keys, const uint32_t *off,
+                                                       const uint32_t *adj, uint8_t *red)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n; p += nw) {
+        const uint64_t hi = keys[p] >> 32;
+        if (p == 0 || (keys[p - 1] >> 32) != hi) continue;
+        // first position of the run: lower bound of hi among keys[0, p)
+        uint32_t lo = 0, up = p;
+        while (lo < up) {
+            const uint32_t mid = lo + (up - lo) / 2;
+            if ((keys[mid] >> 32) < hi) lo = mid + 1;
+            else up = mid;
+        }
+        const uint32_t y = (uint32_t)keys[p];
+        for (uint32_t q = lo; q < p; ++q)
+            if (same_set((uint32_t)keys[q], y, off, adj, lane)) {
+                if (lane == 0) red[y] = 1;
+                break;
+            }
+    }
+}
+
+// flag[x] = 1 for vertices that stay (flag[n] stays 0 for the scan).
+__global__ void __launch_bounds__(256) red_stay_flag_kernel(uint32_t n, const uint8_t *red, uint32_t *flag)
+{
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x)
+        flag[x] = red[x] ? 0u : 1u;
+}
+
+__global__ void __launch_bounds__(256) red_new_id_kernel(uint32_t n, const uint8_t *red, const uint32_t *pos,
+                                                         uint32_t *new_id)
+{
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x)
+        new_id[x] = red[x] ? 0xffffffffu : pos[x];
+}
+
+// 1 + the largest new id on a kept edge.
+__global__ void __launch_bounds__(256) red_top_kernel(const uint32_t *u, const uint32_t *v, const uint64_t *kept,
+                                                      uint64_t k, const uint32_t *new_id, uint32_t *top)
+{
+    uint32_t t = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < k; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t e = kept[i];
+        t = max(t, max(new_id[u[e]], new_id[v[e]]) + 1u);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t = max(t, __shfl_xor_sync(FULLW, t, o));
+    if ((threadIdx.x & 31) == 0 && t) atomicMax(top, t);
+}
+
 }  // namespace
 
 IngestResult ingest_edges(uint64_t m, const uint32_t *du, const uint32_t *dv, const uint8_t *dw, uint32_t n,
@@ -914,5 +1108,124 @@ EdgeTextParser read_edge_file(const char *path, bool weighted, cudaStream_t s)
     return p;
 }
 
-}  // namespace pado
+// ---- graph reductions --------------------------------------------------------
 
+namespace {
+
+// Adjacency entries per vertex (a self-loop counts twice), with the range
+// check both reductions share.
+void entry_degrees(uint64_t m, const uint32_t *du, const uint32_t *dv, uint32_t n, uint32_t *deg, uint32_t *scal,
+                   cudaStream_t s)
+{
+    PADO_CUDA(cudaMemsetAsync(deg, 0, (size_t)n * 4, s));
+    PADO_CUDA(cudaMemsetAsync(scal, 0, 4, s));
+    if (m)
+        PADO_LAUNCH("degree_kernel", s,
+                    degree_kernel<<<grid_for(m, 256, 152u * 8u), 256, 0, s>>>(du, dv, m, n, deg, scal));
+    PADO_CHECK(read_back(scal, s) == 0, PADO_E_ARG, "edge endpoint out of range");
+}
+
+// Indices of the edges with no dropped end, in input order; returns the count.
+uint64_t keep_edges(uint64_t m, const uint32_t *du, const uint32_t *dv, const uint8_t *drop, uint64_t *kept,
+                    cudaStream_t s)
+{
+    if (!m) return 0;
+    PBuf<uint32_t> flag(m + 1, s), sums(scan_sums_needed(m + 1), s);
+    PADO_CUDA(cudaMemsetAsync(flag.p + m, 0, 4, s));
+    PADO_LAUNCH("red_keep_flag_kernel", s,
+                red_keep_flag_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, m, drop, flag.p));
+    exclusive_scan(flag.p, m + 1, sums.p, s);
+    PADO_LAUNCH("red_keep_scatter_kernel", s,
+                red_keep_scatter_kernel<<<grid_for(m, 256), 256, 0, s>>>(flag.p, m, kept));
+    return read_back(flag.p + m, s);
+}
+
+void reduce_limits(uint64_t m, uint32_t n)
+{
+    PADO_CHECK(m < (1ull << 31), PADO_E_ARG, "at most 2^31 - 1 edges");
+    PADO_CHECK(n < (1u << 31), PADO_E_ARG, "fewer than 2^31 vertices");
+    PADO_CHECK(n > 0 || m == 0, PADO_E_ARG, "edge endpoint out of range");
+}
+
+}  // namespace
+
+ReduceResult reduce_degree1(uint64_t m, const uint32_t *du, const uint32_t *dv, uint32_t n, cudaStream_t s,
+                            uint8_t *deleted, uint64_t *kept)
+{
+    reduce_limits(m, n);
+    ReduceResult r;
+    r.n = n;
+    if (!n) return r;
+    PADO_CUDA(cudaMemsetAsync(deleted, 0, n, s));
+    PBuf<uint32_t> scal(1, s), deg(n, s), fill(n, s), nb(2ull * n, s);
+    entry_degrees(m, du, dv, n, deg.p, scal.p, s);
+    fill.zero();
+    if (m)
+        PADO_LAUNCH("red_small_adj_kernel", s,
+                    red_small_adj_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, m, deg.p, fill.p, nb.p));
+    scal.zero();
+    PADO_LAUNCH("red_walk_kernel", s,
+                red_walk_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, deg.p, nb.p, deleted, scal.p));
+    PADO_CHECK(read_back(scal.p, s) == 0, PADO_E_CUDA, "degree-1 chain walk exceeded n steps");
+    r.kept = keep_edges(m, du, dv, deleted, kept, s);
+    PADO_CUDA(cudaStreamSynchronize(s));
+    return r;
+}
+
+ReduceResult reduce_equivalent(uint64_t m, const uint32_t *du, const uint32_t *dv, uint32_t n, cudaStream_t s,
+                               uint8_t *redundant, uint32_t *new_id, uint64_t *kept)
+{
+    reduce_limits(m, n);
+    ReduceResult r;
+    r.n = n;
+    if (!n) return r;
+    PADO_CUDA(cudaMemsetAsync(redundant, 0, n, s));
+    const uint32_t bits = id_bits(n);
+    const uint64_t L = 2 * m;
+    PBuf<uint32_t> scal(1, s), off((uint64_t)n + 1, s), adj(std::max<uint64_t>(L, 1), s);
+    entry_degrees(m, du, dv, n, off.p, scal.p, s);  // degrees in off[0, n), then scanned
+    PADO_CUDA(cudaMemsetAsync(off.p + n, 0, 4, s));
+    {
+        PBuf<uint32_t> osums(scan_sums_needed((uint64_t)n + 1), s);
+        exclusive_scan(off.p, (uint64_t)n + 1, osums.p, s);
+    }
+    SortSpace ws(std::max<uint64_t>(L, n), s);
+    if (L) {  // every vertex's entries, ascending: keys (src, dst) sorted
+        PBuf<uint64_t> keys(L, s);
+        PADO_LAUNCH("red_entry_key_kernel", s,
+                    red_entry_key_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, m, bits, keys.p));
+        const uint64_t *sorted = radix_sort(keys.p, L, 0, 2 * bits, ws, s, true);
+        PADO_LAUNCH("red_extract_kernel", s,
+                    red_extract_kernel<<<grid_for(L, 256), 256, 0, s>>>(sorted, L, (1ull << bits) - 1, adj.p));
+    }
+    {
+        // (hash, id) keys sorted on the hash alone: the sort is stable and
+        // the keys start in id order, so every run of one hash is in id order
+        PBuf<uint64_t> hk(n, s);
+        PADO_LAUNCH("red_hash_kernel", s,
+                    red_hash_kernel<<<grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(n, off.p, adj.p, hk.p));
+        const uint64_t *sorted = radix_sort(hk.p, n, 32, 64, ws, s, true);
+        PADO_LAUNCH("red_twin_kernel", s,
+                    red_twin_kernel<<<grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(n, sorted, off.p, adj.p,
+                                                                                    redundant));
+    }
+    {
+        PBuf<uint32_t> pos((uint64_t)n + 1, s), psums(scan_sums_needed((uint64_t)n + 1), s);
+        PADO_CUDA(cudaMemsetAsync(pos.p + n, 0, 4, s));
+        PADO_LAUNCH("red_stay_flag_kernel", s,
+                    red_stay_flag_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, redundant, pos.p));
+        exclusive_scan(pos.p, (uint64_t)n + 1, psums.p, s);
+        PADO_LAUNCH("red_new_id_kernel", s,
+                    red_new_id_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, redundant, pos.p, new_id));
+    }
+    r.kept = keep_edges(m, du, dv, redundant, kept, s);
+    scal.zero();
+    if (r.kept)
+        PADO_LAUNCH("red_top_kernel", s,
+                    red_top_kernel<<<grid_for(r.kept, 256), 256, 0, s>>>(du, dv, kept, r.kept, new_id, scal.p));
+    r.n_out = read_back(scal.p, s);
+    PADO_CUDA(cudaStreamSynchronize(s));
+    return r;
+}
+
+}  // namespace pado

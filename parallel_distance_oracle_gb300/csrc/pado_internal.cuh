@@ -132,6 +132,21 @@ IngestResult ingest_edges(uint64_t m, const uint32_t *d_u, const uint32_t *d_v, 
 // graph.h:176-206).  With rank, *rank_out receives it on the device.
 DevGraph prepare_csr(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, const uint32_t *rank,
                      cudaStream_t s, DBuf<uint32_t> *rank_out);
+// Graph reductions of the reference's conversion tools (ingest.cu), over an
+// edge list in device memory with ids < n: per-vertex flags (n bytes), the
+// indices of the surviving edges in input order (room for m), and for the
+// equivalence reduction the new ids (n entries).  Stream-ordered; return when
+// the outputs are written.
+struct ReduceResult {
+    uint32_t n = 0;     // vertices
+    uint64_t kept = 0;  // surviving edges
+    uint32_t n_out = 0; // equivalence: 1 + the largest new id on a kept edge
+};
+ReduceResult reduce_degree1(uint64_t m, const uint32_t *du, const uint32_t *dv, uint32_t n, cudaStream_t s,
+                            uint8_t *deleted, uint64_t *kept);
+ReduceResult reduce_equivalent(uint64_t m, const uint32_t *du, const uint32_t *dv, uint32_t n, cudaStream_t s,
+                               uint8_t *redundant, uint32_t *new_id, uint64_t *kept);
+
 // Trims the ingest scratch pool of the current device to keep_bytes.
 void release_scratch(uint64_t keep_bytes);
 // b[i] = a[i] for i < n (device arrays, stream-ordered).

@@ -127,6 +127,66 @@ def grid_with_shortcuts(n: int, frac: float, seed: int) -> CSRGraph:
     return csr_from_edges(n, np.concatenate([u, su]), np.concatenate([v, sv]))
 
 
+def reduction_edges(n: int, seed: int, iso_path_max: int = 4):
+    """An edge list ``(u, v)`` (uint32, ids < n, input order) rich in what the
+    reference's reduction tools remove: a sparse random core on half the
+    vertices, pendant paths of 1-6 vertices and pendant stars hung on it,
+    cliques of 3-5 vertices joined to the core by one member (the others have
+    equal closed neighbourhoods), isolated paths of 2..iso_path_max vertices,
+    and about 1% repeated edges and 0.5% self-loops.  Ids are shuffled and
+    the edges put in random order.  (On an isolated path of four or more
+    vertices the reference's degree-1 tool can walk for ever, depending on
+    the edge order.)"""
+    rng = _rng(seed)
+    core = max(n // 2, 2)
+    us = list(rng.integers(0, core, 2 * core))
+    vs = list(rng.integers(0, core, 2 * core))
+    nxt = core
+
+    def add(a, b):
+        us.append(a)
+        vs.append(b)
+
+    while nxt < n:
+        kind = rng.random()
+        if kind < 0.45:  # pendant path
+            prev = int(rng.integers(0, core))
+            for _ in range(int(rng.integers(1, 7))):
+                if nxt >= n:
+                    break
+                add(prev, nxt)
+                prev, nxt = nxt, nxt + 1
+        elif kind < 0.6:  # pendant star
+            hub = int(rng.integers(0, core))
+            for _ in range(int(rng.integers(2, 6))):
+                if nxt >= n:
+                    break
+                add(hub, nxt)
+                nxt += 1
+        elif kind < 0.85:  # clique with one member on the core
+            k = min(int(rng.integers(3, 6)), n - nxt)
+            mem = list(range(nxt, nxt + k))
+            nxt += k
+            for i in range(k):
+                for j in range(i + 1, k):
+                    add(mem[i], mem[j])
+            add(mem[0], int(rng.integers(0, core)))
+        else:  # isolated path (a single edge when it has two vertices)
+            k = min(int(rng.integers(2, iso_path_max + 1)), n - nxt)
+            for i in range(k - 1):
+                add(nxt + i, nxt + i + 1)
+            nxt += k
+    u = np.array(us, dtype=np.int64)
+    v = np.array(vs, dtype=np.int64)
+    rep = rng.integers(0, len(u), size=max(len(u) // 100, 1))
+    loops = rng.integers(0, n, size=max(n // 200, 1))
+    u = np.concatenate([u, u[rep], loops])
+    v = np.concatenate([v, v[rep], loops])
+    perm = rng.permutation(n)
+    order = rng.permutation(len(u))
+    return perm[u[order]].astype(np.uint32), perm[v[order]].astype(np.uint32)
+
+
 def path_graph(n: int) -> CSRGraph:
     i = np.arange(n - 1, dtype=np.int64)
     return csr_from_edges(n, i, i + 1)

@@ -454,6 +454,65 @@ def graph_ingest(u, v, w=None, n: int | None = None, dedupe: bool = False):
     return CSRGraph(n, off, adj[:e].copy(), None if wo is None else wo[:e].copy()), rank[:n]
 
 
+def _edge_arrays(u, v, n):
+    u, v = _u32(u), _u32(v)
+    if len(u) != len(v):
+        raise ValueError("edge arrays differ in length")
+    if n is None:
+        n = int(max(u.max(initial=0), v.max(initial=0))) + 1 if len(u) else 0
+    return u, v, len(u), n
+
+
+def reduce_degree1(u, v, n: int | None = None):
+    """The reference's degree-1 chain deletion
+    (tools/pseudocode-delete_1-degree_vertices.cpp) on the device
+    (pado_reduce_degree1).  ``n`` defaults to max id + 1, as the tool sets it.
+    Returns ``(deleted, kept)``: uint8 flags per vertex and the indices of the
+    input edges the tool writes, in input order."""
+    u, v, m, n = _edge_arrays(u, v, n)
+    deleted = np.zeros(max(n, 1), np.uint8)
+    kept = np.zeros(max(m, 1), np.uint64)
+    k = C.c_uint64()
+    check(lib.pado_reduce_degree1(m, ptr(u), ptr(v), n, ptr(deleted), ptr(kept), C.byref(k)))
+    return deleted[:n], kept[:k.value].copy()
+
+
+def reduce_equivalent(u, v, n: int | None = None):
+    """The reference's equivalent-vertex removal
+    (distributed_version/tools/graph-convert/remove_equivalent_vertices.cpp)
+    on the device (pado_reduce_equivalent).  Returns ``(redundant, new_id,
+    kept, n_out)``: flags, new ids of the vertices that stay (2^32 - 1 for the
+    others), indices of the kept input edges and the vertex count the tool
+    writes."""
+    u, v, m, n = _edge_arrays(u, v, n)
+    red = np.zeros(max(n, 1), np.uint8)
+    nid = np.zeros(max(n, 1), np.uint32)
+    kept = np.zeros(max(m, 1), np.uint64)
+    k, nout = C.c_uint64(), C.c_uint32()
+    check(lib.pado_reduce_equivalent(m, ptr(u), ptr(v), n, ptr(red), ptr(nid), ptr(kept), C.byref(k),
+                                     C.byref(nout)))
+    return red[:n], nid[:n], kept[:k.value].copy(), int(nout.value)
+
+
+def write_degree1_output(path, u, v, kept) -> None:
+    """The delete_1-degree tool's output file: the kept edges as "head tail"
+    lines, in input order."""
+    u, v = _u32(u), _u32(v)
+    with open(path, "w") as f:
+        f.write("".join(f"{a} {b}\n" for a, b in zip(u[kept].tolist(), v[kept].tolist())))
+
+
+def write_equivalent_output(path, u, v, new_id, kept, n_out: int) -> None:
+    """The remove_equivalent_vertices tool's binary file: num_v (uint32),
+    num_e (uint64), then (new_id[head], new_id[tail]) uint32 pairs."""
+    u, v = _u32(u), _u32(v)
+    pairs = np.stack([new_id[u[kept]], new_id[v[kept]]], 1).astype(np.uint32)
+    with open(path, "wb") as f:
+        f.write(np.uint32(n_out).tobytes())
+        f.write(np.uint64(len(kept)).tobytes())
+        f.write(pairs.tobytes())
+
+
 def parse_edge_text(text: bytes, weighted: bool = False):
     """Edge-list text to arrays on the device (pado_edge_text_parse), with the
     line rules of Graph(filename) (graph.h:95-117): returns ``(u, v, w)``,
