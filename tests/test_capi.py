@@ -15,7 +15,7 @@ HEADER = Path(__file__).resolve().parents[1] / "include" / "pado_gpu.h"
 
 def declared_functions():
     text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
-    return sorted(set(re.findall(r"\b(pado_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(pado_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_header_declares_what_binding_knows():
