@@ -66,6 +66,12 @@ SERVE = dict(budget=40 << 30, graphs=64, kmax=65536, zipf=1.1, rates=(1e4, 3e4, 
 # side is the reference's Graph(edge_list) + id_transfer on the s18 samples.
 INGEST = dict(scale=20, ef=16, seed=2, ref_scale=18, scratch_cache=2 << 30,
               desc="raw R-MAT s20 ef16 samples -> Graph::construct + degree rank + id_transfer (no dedupe)")
+# Graph reductions (the reference's two conversion tools): the same raw
+# R-MAT s20/ef16 samples through degree-1 chain deletion and equivalent-vertex
+# removal; the CPU side is the oracle's restatement on the s18 samples.
+REDUCE = dict(scale=20, ef=16, seed=2, ref_scale=18,
+              desc="raw R-MAT s20 ef16 samples -> degree-1 chain deletion + equivalent-vertex removal "
+                   "(tools/pseudocode-delete_1-degree_vertices.cpp, remove_equivalent_vertices.cpp)")
 METRIC = "labels_per_s"
 UNIT = "labels/s"
 
@@ -227,7 +233,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rmat20", choices=sorted(WORKLOADS) + ["many", "serve", "ingest"])
+    ap.add_argument("--workload", default="rmat20",
+                    choices=sorted(WORKLOADS) + ["many", "serve", "ingest", "reduce"])
     ap.add_argument("--many-graphs", type=int, default=MANY["graphs"])
     ap.add_argument("--many-nmax", type=int, default=MANY["n_hi"])
     ap.add_argument("--many-batch", type=int, default=0, help="skip tuning and use this batch size")
@@ -245,6 +252,8 @@ def main():
         return run_serve(args)
     if args.workload == "ingest":
         return run_ingest(args)
+    if args.workload == "reduce":
+        return run_reduce(args)
     wl = WORKLOADS[args.workload]
     if args.ref_batches is None:
         args.ref_batches = wl["ref_batches"]
@@ -745,6 +754,187 @@ def attribute_loop_bytes(prof):
                         ("w_loop_kernel", ("w_pull_kernel", "w_mark_kernel"))):
         if loop in prof:
             prof[loop]["bytes"] = sum(prof.get(k, {}).get("bytes", 0) for k in parts)
+
+
+def reduce_edges_sample(scale: int):
+    n, u, v, _ = G.rmat_edges(scale, REDUCE["ef"], REDUCE["seed"])
+    u, v = u.astype(np.uint32), v.astype(np.uint32)
+    return int(max(u.max(), v.max())) + 1, u, v
+
+
+def reduce_cpu(scale: int):
+    """The oracle's restatement of both tools on the raw samples at `scale`
+    (the reference's tools read and write files, so they are not timed);
+    returns (edges/s, seconds, edges)."""
+    from oracle import orc
+    n, u, v = reduce_edges_sample(scale)
+    t0 = time.perf_counter()
+    orc.reduce_degree1(u, v, n)
+    orc.reduce_equivalent(u, v, n)
+    sec = time.perf_counter() - t0
+    return len(u) / sec, sec, len(u)
+
+
+def reduce_kernel_bytes(kernel: str, m: int, n: int, prof_launches: int):
+    """Algorithmic bytes of all launches of `kernel` in one step (both
+    reductions): reads + writes each launch must make once."""
+    bits = 1
+    while (1 << bits) < n:
+        bits += 1
+    entry_passes = (2 * bits + 7) // 8
+    L = 2 * m
+    table = {
+        # the entry sort (L keys) and the hash sort (n keys, 4 passes): 8 B read + 8 B written per key per pass
+        "rs_scatter_kernel.aux": 16 * (entry_passes * L + 4 * n),
+        "rs_hist_kernel.aux": 8 * (entry_passes * L + 4 * n),
+        "degree_kernel": 2 * (8 * m + 4 * n),          # once per reduction: edges in, counters out
+        "red_entry_key_kernel": 8 * m + 8 * L,
+        "red_extract_kernel": 12 * L,
+        "red_hash_kernel": 4 * L + 8 * n + 8 * n,      # entries, offsets, keys out
+        "red_small_adj_kernel": 8 * m + 8 * m,         # edges, degree lookups (lower bound)
+        "red_keep_flag_kernel": 2 * (8 * m + 2 * m + 4 * m),
+        "red_keep_scatter_kernel": 2 * (4 * m),
+    }
+    return table.get(kernel)
+
+
+def run_reduce(args):
+    """Both graph reductions on the raw R-MAT s20 samples.  value = input
+    edges/s of degree-1 deletion + equivalent-vertex removal with the edge
+    arrays resident in HBM (the _device entries, CUDA events); e2e = the same
+    through the host-array entries, wall clock."""
+    world, grank, local = dist_setup(args)
+    if args.impl == "reference":
+        if grank != 0:
+            return
+        vals, secs, m = [], [], 0
+        for i in range(args.warmup + args.steps):
+            v, sec, m = reduce_cpu(REDUCE["ref_scale"])
+            if i >= args.warmup:
+                vals.append(v)
+                secs.append(sec)
+            log(f"reference step {i}: {m} edges in {sec:.2f}s (port)")
+        v = statistics.mean(vals)
+        sample = f"raw R-MAT s{REDUCE['ref_scale']} ef16 samples ({m} edges) per step, both reductions"
+        print(json.dumps({"metric": "edges_per_s", "value": v, "unit": "edges/s", "impl": "reference",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": statistics.mean(secs) * 1e3, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                          "config": {"workload": "reduce", "desc": REDUCE["desc"]},
+                          "cpu_baseline": {"value": v, "unit": "edges/s", "cores": 1, "kind": "port",
+                                           "sample": sample},
+                          "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    from parallel_distance_oracle_gb300 import _lib
+    lib = _lib.lib
+    n, u, v = reduce_edges_sample(REDUCE["scale"])
+    m = len(u)
+    log(f"reduce: {m} edges, n = {n}")
+    du = torch.from_numpy(u.view(np.int32)).cuda()
+    dv = torch.from_numpy(v.view(np.int32)).cuda()
+    d_flag = torch.empty(n, dtype=torch.uint8, device="cuda")
+    d_nid = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_kept = torch.empty(m, dtype=torch.int64, device="cuda")
+    hu = torch.from_numpy(u.view(np.int32)).pin_memory()
+    hv = torch.from_numpy(v.view(np.int32)).pin_memory()
+    h_del = torch.empty(n, dtype=torch.uint8).pin_memory()
+    h_red = torch.empty(n, dtype=torch.uint8).pin_memory()
+    h_nid = torch.empty(n, dtype=torch.int32).pin_memory()
+    h_kept = torch.empty(m, dtype=torch.int64).pin_memory()
+    stream = torch.cuda.current_stream()
+    k1, k2, nout = C.c_uint64(), C.c_uint64(), C.c_uint32()
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def dev_once():
+        _lib.check(lib.pado_reduce_degree1_device(m, P(du), P(dv), n, P(d_flag), P(d_kept), C.byref(k1),
+                                                  C.c_void_p(stream.cuda_stream)))
+        _lib.check(lib.pado_reduce_equivalent_device(m, P(du), P(dv), n, P(d_flag), P(d_nid), P(d_kept),
+                                                     C.byref(k2), C.byref(nout), C.c_void_p(stream.cuda_stream)))
+
+    def host_once():
+        _lib.check(lib.pado_reduce_degree1(m, P(hu), P(hv), n, P(h_del), P(h_kept), C.byref(k1)))
+        _lib.check(lib.pado_reduce_equivalent(m, P(hu), P(hv), n, P(h_red), P(h_nid), P(h_kept), C.byref(k2),
+                                              C.byref(nout)))
+
+    _lib.check(lib.pado_set_scratch_cache(INGEST["scratch_cache"]))
+    for _ in range(args.warmup):
+        dev_once()
+        host_once()
+    torch.cuda.synchronize()
+    log(f"degree-1 keeps {k1.value} edges ({int(h_del.sum())} vertices deleted); equivalence keeps {k2.value} "
+        f"edges ({int(h_red.sum())} vertices redundant, {nout.value} written)")
+    launches0 = lib.pado_kernel_launches()
+    dev_s, wall_s = [], []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for i in range(args.steps):
+            torch.cuda.synchronize()
+            e0.record(stream)
+            dev_once()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            dev_s.append(e0.elapsed_time(e1) / 1e3)
+            t0 = time.perf_counter()
+            host_once()
+            wall_s.append(time.perf_counter() - t0)
+            log(f"step {i}: device-resident {dev_s[-1] * 1e3:.2f} ms, host arrays {wall_s[-1] * 1e3:.2f} ms")
+    launches = lib.pado_kernel_launches() - launches0
+    clocks = clk.summary()
+    dev_mean, wall_mean = statistics.mean(dev_s), statistics.mean(wall_s)
+    if pg:
+        dev_mean, wall_mean = max_over_ranks(pg, [dev_mean, wall_mean], "cuda")
+    prof, roofline = {}, None
+    if not args.no_profile:
+        _lib.check(lib.pado_profile(2))
+        dev_once()
+        torch.cuda.synchronize()
+        prof = read_profile(lib)
+        _lib.check(lib.pado_profile(0))
+    _lib.check(lib.pado_set_scratch_cache(0))
+    peak, peak_src = peaks()
+    if prof:
+        tot_ms = sum(x["ms"] for x in prof.values())
+        top = max(prof, key=lambda k: prof[k]["ms"])
+        tk = prof[top]
+        tot_bytes = reduce_kernel_bytes(top, m, n, tk["launches"])
+        per = tot_bytes / tk["launches"] if tot_bytes else None
+        avg_s = tk["ms"] / 1e3 / max(tk["launches"], 1)
+        ach = per / avg_s / 1e9 if per else None
+        roofline = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": ach / peak if ach else None, "traffic": traffic_from_profiles(top, "reduce"),
+                    "peak_source": peak_src, "share_of_reduce_device_time": tk["ms"] / tot_ms if tot_ms else None,
+                    "launches": tk["launches"], "avg_launch_us": avg_s * 1e6, "bytes_per_launch": per}
+    cpu = None
+    if not args.no_cpu_baseline and grank == 0:
+        cv, sec, cm = reduce_cpu(REDUCE["ref_scale"])
+        cpu = {"value": cv, "unit": "edges/s", "cores": 1, "kind": "port", "seconds": sec,
+               "sample": f"raw R-MAT s{REDUCE['ref_scale']} ef16 samples ({cm} edges), both reductions"}
+    if grank == 0:
+        h2d = 2 * 8 * m
+        d2h = 2 * n + 4 * n + 8 * (k1.value + k2.value)
+        print(json.dumps({
+            "metric": "edges_per_s", "value": m * world / dev_mean, "unit": "edges/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_mean * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": "reduce", "desc": REDUCE["desc"], "edges": m, "n": n,
+                       "l2": f"inputs larger than L2 ({8 * m / 1e6:.0f} MB of edges, {16 * m / 1e6:.0f} MB of "
+                             f"entry keys)", "parallelism": f"replicas x{world}"},
+            "degree1": {"kept_edges": k1.value, "deleted_vertices": int(h_del.sum())},
+            "equivalent": {"kept_edges": k2.value, "redundant_vertices": int(h_red.sum()), "n_out": nout.value},
+            "e2e": {"value": m * world / wall_mean, "unit": "edges/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "wall_s": wall_mean},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
+            "profile": prof}), flush=True)
+    if pg:
+        pg.destroy_process_group()
 
 
 def read_profile(lib):

@@ -1,5 +1,6 @@
 // ingest.cu -- from an edge-list text or an undirected edge list to the
-// ranked CSR the labelers take, on the device.
+// ranked CSR the labelers take, on the device; and the reference's two
+// graph-reduction tools over the same edge lists (the last section).
 //
 // The reference prepares its graph on the host before labeling:
 //   Graph(const char *) / WeightedGraph(const char *) (graph.h:95-117,
