@@ -787,10 +787,11 @@ def reduce_kernel_bytes(kernel: str, m: int, n: int, prof_launches: int):
         # the entry sort (L keys) and the hash sort (n keys, 4 passes): 8 B read + 8 B written per key per pass
         "rs_scatter_kernel.aux": 16 * (entry_passes * L + 4 * n),
         "rs_hist_kernel.aux": 8 * (entry_passes * L + 4 * n),
-        "degree_kernel": 2 * (8 * m + 4 * n),          # once per reduction: edges in, counters out
+        "degree_kernel": 8 * m + 4 * n,                # degree-1 only: edges in, counters out
         "red_entry_key_kernel": 8 * m + 8 * L,
-        "red_extract_kernel": 12 * L,
-        "red_hash_kernel": 4 * L + 8 * n + 8 * n,      # entries, offsets, keys out
+        "red_extract_hash_kernel": 12 * L + 8 * n,     # sorted keys in, adjacency out, one sum per vertex
+        "red_offsets_kernel": 8 * L + 4 * n,
+        "red_hash_finish_kernel": 24 * n,
         "red_small_adj_kernel": 8 * m + 8 * m,         # edges, degree lookups (lower bound)
         "red_keep_flag_kernel": 2 * (8 * m + 2 * m + 4 * m),
         "red_keep_scatter_kernel": 2 * (4 * m),

@@ -702,22 +702,18 @@ __global__ void __launch_bounds__(256) red_keep_scatter_kernel(const uint32_t *p
         if (pos[e + 1] != pos[e]) kept[pos[e]] = e;
 }
 
-// Both adjacency entries of every edge as (src << bits | dst) keys.
+// Both adjacency entries of every edge as (src << bits | dst) keys; ids must
+// be below n (a flag otherwise).
 __global__ void __launch_bounds__(256) red_entry_key_kernel(const uint32_t *u, const uint32_t *v, uint64_t m,
-                                                            uint32_t bits, uint64_t *keys)
+                                                            uint32_t n, uint32_t bits, uint64_t *keys,
+                                                            uint32_t *bad)
 {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t a = u[e], b = v[e];
+        if (a >= n || b >= n) atomicOr(bad, 1u);
         keys[2 * e] = a << bits | b;
         keys[2 * e + 1] = b << bits | a;
     }
-}
-
-__global__ void __launch_bounds__(256) red_extract_kernel(const uint64_t *keys, uint64_t L, uint64_t mask,
-                                                          uint32_t *adj)
-{
-    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < L; k += (uint64_t)gridDim.x * blockDim.x)
-        adj[k] = (uint32_t)(keys[k] & mask);
 }
 
 // SplitMix64's output function (Steele, Lea and Flood, "Fast splittable
@@ -730,26 +726,57 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x)
     return x ^ (x >> 31);
 }
 
-// A warp per vertex x: a hash of the multiset {x} + its entries (a sum of
-// mixed elements does not depend on their order), folded with the set size
-// into 32 bits, as the key (hash << 32 | x).  Equal sets have equal upper
-// halves; the converse is checked exactly afterwards.
-__global__ void __launch_bounds__(256) red_hash_kernel(uint32_t n, const uint32_t *off, const uint32_t *adj,
-                                                       uint64_t *keys)
+// The sorted entries: adjacency out, and per source vertex the sum of its
+// entries' mixed values (a sum does not depend on order).  A warp takes 32
+// consecutive entries; equal sources are contiguous, so a segmented scan over
+// the lanes sums each run and its last lane adds the run with one atomic.
+__global__ void __launch_bounds__(256) red_extract_hash_kernel(const uint64_t *keys, uint64_t L, uint32_t bits,
+                                                               uint32_t *adj, unsigned long long *h)
 {
     const int lane = threadIdx.x & 31;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; x < n; x += nw) {
-        const uint32_t b = off[x], e = off[x + 1];
-        uint64_t h = 0;
-        for (uint32_t k = b + lane; k < e; k += 32) h += mix64(adj[k]);
+    const uint64_t mask = (1ull << bits) - 1;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t base = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < L; base += nw * 32) {
+        const uint64_t k = base + lane;
+        const bool live = k < L;
+        const uint64_t key = live ? keys[k] : 0ull;
+        const uint32_t src = live ? (uint32_t)(key >> bits) : 0xffffffffu;
+        if (live) adj[k] = (uint32_t)(key & mask);
+        uint64_t c = live ? mix64(key & mask) : 0ull;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(FULLW, h, o);
-        if (lane == 0) {
-            h += mix64(x);
-            const uint64_t f = mix64(h ^ ((uint64_t)(e - b + 1) << 40));
-            keys[x] = (f >> 32) << 32 | x;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t t = __shfl_up_sync(FULLW, c, o);
+            const uint32_t s2 = __shfl_up_sync(FULLW, src, o);
+            if (lane >= o && s2 == src) c += t;
         }
+        const uint32_t nsrc = __shfl_down_sync(FULLW, src, 1);
+        if (live && (lane == 31 || nsrc != src)) atomicAdd(&h[src], (unsigned long long)c);
+    }
+}
+
+// Offsets of the sorted entries' sources: thread k (0 <= k <= L) writes
+// off[x] = k for every x in (src(k-1), src(k)], with src(-1) = -1 and
+// src(L) = n, so vertices without entries get the next start and off[n] = L.
+__global__ void __launch_bounds__(256) red_offsets_kernel(const uint64_t *keys, uint64_t L, uint32_t bits,
+                                                          uint32_t n, uint32_t *off)
+{
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k <= L; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t cur = k < L ? (uint32_t)(keys[k] >> bits) : n;
+        const int64_t prev = k > 0 ? (int64_t)(keys[k - 1] >> bits) : -1;
+        for (int64_t x = prev + 1; x <= (int64_t)cur; ++x) off[x] = (uint32_t)k;
+    }
+}
+
+// The set hash of every vertex x: its entries' sum plus x itself, folded
+// with the set size into 32 bits, as the key (hash << 32 | x).  Equal sets
+// have equal upper halves; the converse is checked exactly afterwards.
+__global__ void __launch_bounds__(256) red_hash_finish_kernel(uint32_t n, const uint32_t *off,
+                                                              const unsigned long long *h, uint64_t *keys)
+{
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        const uint64_t sum = (uint64_t)h[x] + mix64(x);
+        const uint64_t f = mix64(sum ^ ((uint64_t)(off[x + 1] - off[x] + 1) << 40));
+        keys[x] = (f >> 32) << 32 | x;
     }
 }
 
@@ -1184,27 +1211,32 @@ ReduceResult reduce_equivalent(uint64_t m, const uint32_t *du, const uint32_t *d
     const uint32_t bits = id_bits(n);
     const uint64_t L = 2 * m;
     PBuf<uint32_t> scal(1, s), off((uint64_t)n + 1, s), adj(std::max<uint64_t>(L, 1), s);
-    entry_degrees(m, du, dv, n, off.p, scal.p, s);  // degrees in off[0, n), then scanned
-    PADO_CUDA(cudaMemsetAsync(off.p + n, 0, 4, s));
-    {
-        PBuf<uint32_t> osums(scan_sums_needed((uint64_t)n + 1), s);
-        exclusive_scan(off.p, (uint64_t)n + 1, osums.p, s);
-    }
+    PBuf<unsigned long long> h(n, s);
+    h.zero();
     SortSpace ws(std::max<uint64_t>(L, n), s);
-    if (L) {  // every vertex's entries, ascending: keys (src, dst) sorted
-        PBuf<uint64_t> keys(L, s);
-        PADO_LAUNCH("red_entry_key_kernel", s,
-                    red_entry_key_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, m, bits, keys.p));
-        const uint64_t *sorted = radix_sort(keys.p, L, 0, 2 * bits, ws, s, true);
-        PADO_LAUNCH("red_extract_kernel", s,
-                    red_extract_kernel<<<grid_for(L, 256), 256, 0, s>>>(sorted, L, (1ull << bits) - 1, adj.p));
+    {
+        // every vertex's entries, ascending: keys (src, dst) sorted; then the
+        // adjacency, the entry sums of the set hashes and the offsets
+        PBuf<uint64_t> keys(std::max<uint64_t>(L, 1), s);
+        const uint64_t *sorted = keys.p;
+        if (L) {
+            scal.zero();
+            PADO_LAUNCH("red_entry_key_kernel", s,
+                        red_entry_key_kernel<<<grid_for(m, 256), 256, 0, s>>>(du, dv, m, n, bits, keys.p, scal.p));
+            PADO_CHECK(read_back(scal.p, s) == 0, PADO_E_ARG, "edge endpoint out of range");
+            sorted = radix_sort(keys.p, L, 0, 2 * bits, ws, s, true);
+            PADO_LAUNCH("red_extract_hash_kernel", s,
+                        red_extract_hash_kernel<<<grid_for(L, 256), 256, 0, s>>>(sorted, L, bits, adj.p, h.p));
+        }
+        PADO_LAUNCH("red_offsets_kernel", s,
+                    red_offsets_kernel<<<grid_for(L + 1, 256), 256, 0, s>>>(sorted, L, bits, n, off.p));
     }
     {
         // (hash, id) keys sorted on the hash alone: the sort is stable and
         // the keys start in id order, so every run of one hash is in id order
         PBuf<uint64_t> hk(n, s);
-        PADO_LAUNCH("red_hash_kernel", s,
-                    red_hash_kernel<<<grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(n, off.p, adj.p, hk.p));
+        PADO_LAUNCH("red_hash_finish_kernel", s,
+                    red_hash_finish_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, off.p, h.p, hk.p));
         const uint64_t *sorted = radix_sort(hk.p, n, 32, 64, ws, s, true);
         PADO_LAUNCH("red_twin_kernel", s,
                     red_twin_kernel<<<grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(n, sorted, off.p, adj.p,
