@@ -136,7 +136,8 @@ def reduction_edges(n: int, seed: int, iso_path_max: int = 4):
     and about 1% repeated edges and 0.5% self-loops.  Ids are shuffled and
     the edges put in random order.  (On an isolated path of four or more
     vertices the reference's degree-1 tool can walk for ever, depending on
-    the edge order.)"""
+    the edge order; a core vertex left without core edges turns the pendant
+    paths hung on it into such a path too.)"""
     rng = _rng(seed)
     core = max(n // 2, 2)
     us = list(rng.integers(0, core, 2 * core))

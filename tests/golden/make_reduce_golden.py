@@ -9,7 +9,8 @@ count and (head, tail) pairs of the binary file the equivalence tool writes.
 
 Inputs on which the reference's degree-1 walk would never end (the oracle
 reports them; isolated paths of four or more vertices can do it, so the mixed
-cases keep theirs shorter) are not given to it.  Needs the reference tree and g++.
+cases keep theirs shorter, and a case that still has one is skipped) are not
+given to it.  Needs the reference tree and g++.
 Usage:  python tests/golden/make_reduce_golden.py
 """
 from __future__ import annotations
