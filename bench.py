@@ -22,7 +22,6 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
 import time
 from pathlib import Path
 
@@ -775,7 +774,7 @@ def reduce_cpu(scale: int):
     return len(u) / sec, sec, len(u)
 
 
-def reduce_kernel_bytes(kernel: str, m: int, n: int, prof_launches: int):
+def reduce_kernel_bytes(kernel: str, m: int, n: int):
     """Algorithmic bytes of all launches of `kernel` in one step (both
     reductions): reads + writes each launch must make once."""
     bits = 1
@@ -905,7 +904,7 @@ def run_reduce(args):
         tot_ms = sum(x["ms"] for x in prof.values())
         top = max(prof, key=lambda k: prof[k]["ms"])
         tk = prof[top]
-        tot_bytes = reduce_kernel_bytes(top, m, n, tk["launches"])
+        tot_bytes = reduce_kernel_bytes(top, m, n)
         per = tot_bytes / tk["launches"] if tot_bytes else None
         avg_s = tk["ms"] / 1e3 / max(tk["launches"], 1)
         ach = per / avg_s / 1e9 if per else None

@@ -2,7 +2,6 @@
 where the reference tree is available, the reference's unmodified pado.cpp and
 query_distance.cpp with their labeler headers mapped to include/pado_gpu.hpp."""
 import os
-import subprocess
 from pathlib import Path
 
 import pytest
