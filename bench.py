@@ -45,6 +45,9 @@ WORKLOADS = {
     # weighted R-MAT s18/ef8, weights 1..100, batch 512
     "wrmat18": dict(kind="w", scale=18, ef=8, seed=3, K=0, B=512, queries=1_000_000, qseed=13, ref_batches=0,
                     desc="weighted R-MAT s18 ef8, weights U[1,100], degree order, B=512"),
+    # a smaller case of the weighted kernels, sized for ncu captures
+    "wrmat16": dict(kind="w", scale=16, ef=8, seed=3, K=0, B=512, queries=1_000_000, qseed=13, ref_batches=0,
+                    desc="weighted R-MAT s16 ef8, weights U[1,100], degree order, B=512 (profiling case)"),
 }
 # Many independent graphs labeled together: 512 graphs, n log-uniform in
 # [1,000, n_hi], half Erdos-Renyi (average degree 6), half 2D grids with 2%

@@ -264,8 +264,12 @@ template <inti BATCH_SIZE = 512>
 using WeightedParaVertexCentricPLL = WeightedVertexCentricPLL<BATCH_SIZE>;
 
 // The AVX-512 classes of the reference (pado_unw_vec_{unp,para}.h,
-// pado_weighted_vec_{unp,para}.h; pado.cpp's -v 1 modes) compute the same
-// labels as the scalar ones, so they map onto the same GPU labelers.
+// pado_weighted_vec_{unp,para}.h; pado.cpp's -v 1 modes) map onto the same GPU
+// labelers, which produce the scalar classes' labels.  The weighted AVX-512
+// classes produce exactly those labels.  The unweighted ones agree except that,
+// on some graphs, they leave out the distance-1 label of a degree-1 vertex to
+// its only neighbour, so their own query answers unreachable for that adjacent
+// pair; a -v 1 user gets the scalar (correct) labels here.
 template <inti BATCH_SIZE = 1024>
 using VertexCentricPLLVec = VertexCentricPLL<BATCH_SIZE>;
 template <inti BATCH_SIZE = 1024>

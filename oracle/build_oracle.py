@@ -17,9 +17,12 @@ Two products, both git-ignored build outputs:
        force-included ``ref_prelude.h`` supplies them on x86 and stand-ins
        elsewhere);
     3. the class constant ``BITPARALLEL_SIZE = 50`` becomes the macro
-       ``PADO_REF_BP_SIZE`` so that the 64-root configuration can be built.
-  Staging needs the reference tree (``PADO_REFERENCE_DIR``, default: the
-  mounted reference); compiling only needs the staged copy, so a host that
+       ``PADO_REF_BP_SIZE`` so that the 64-root configuration can be built;
+    4. ``load_index_from_file`` reads the file's root count into a local
+       instead of into that constant (pado_unw_unv_unp.h:1194 writes to a
+       ``static const`` and faults), so the reference can read index files.
+  Staging needs the reference tree (``PADO_REFERENCE_DIR``, default: a
+  ``reference`` directory beside the repository); compiling only needs the staged copy, so a host that
   received ``oracle/_ref/inc`` can build the driver without the tree.
 * ``oracle/_ref/delete_1_degree`` and ``oracle/_ref/remove_equivalent`` -- the
   reference's two graph-conversion tools (``tools/pseudocode-delete_1-degree_
@@ -52,10 +55,13 @@ REF_HEADERS = [
     "pado_weighted_unv_para.h",
 ]
 REF_BP_SIZES = (50, 64)
+# The AVX-512 classes (pado.cpp's `-v 1` modes) and their helper header.
+REF_VEC_HEADERS = ["avx512_pado.h", "pado_unw_vec_unp.h", "pado_unw_vec_para.h", "pado_weighted_vec_unp.h",
+                   "pado_weighted_vec_para.h"]
 
 
 def _reference_dir() -> Path:
-    return Path(os.environ.get("PADO_REFERENCE_DIR", "/root/reference"))
+    return Path(os.environ.get("PADO_REFERENCE_DIR", ORACLE_DIR.parent.parent / "reference"))
 
 
 def _newer(out: Path, *inputs: Path) -> bool:
@@ -81,6 +87,10 @@ def _patch(text: str) -> str:
     text = re.sub(r"^\s*#include\s*<(xmmintrin|immintrin)\.h>\s*$", "", text, flags=re.M)
     text = text.replace("static const inti BITPARALLEL_SIZE = 50;",
                         "static const inti BITPARALLEL_SIZE = PADO_REF_BP_SIZE;")
+    # load_index_from_file reads the file's root count into the class constant
+    # (a write to read-only storage: it faults); read it into a local instead
+    text = text.replace("fin.read((char *) &BITPARALLEL_SIZE, sizeof(BITPARALLEL_SIZE));",
+                        "{ inti bp_size_in_file = 0; fin.read((char *) &bp_size_in_file, sizeof(bp_size_in_file)); }")
     return text
 
 
@@ -96,7 +106,7 @@ def stage_reference() -> bool:
     if not src.is_dir():
         return False
     REF_INC.mkdir(parents=True, exist_ok=True)
-    for name in REF_HEADERS:
+    for name in REF_HEADERS + REF_VEC_HEADERS:
         out = REF_INC / name
         text = _patch((src / name).read_text(errors="replace"))
         if not out.exists() or out.read_text(errors="replace") != text:
@@ -120,7 +130,7 @@ def build_reference(force: bool = False, sizes=REF_BP_SIZES) -> list[Path]:
     stage_reference()
     if not all((REF_INC / h).exists() for h in REF_HEADERS):
         return []
-    deps = [ORACLE_DIR / "ref_driver.cpp", ORACLE_DIR / "ref_prelude.h"] + [REF_INC / h for h in REF_HEADERS]
+    deps = [ORACLE_DIR / "ref_driver.cpp", ORACLE_DIR / "ref_prelude.h", Path(__file__)] + [REF_INC / h for h in REF_HEADERS]
     procs = []
     outs = []
     for k in sizes:
@@ -128,7 +138,11 @@ def build_reference(force: bool = False, sizes=REF_BP_SIZES) -> list[Path]:
         outs.append(out)
         if not force and _newer(out, *deps):
             continue
-        cmd = ["g++", "-std=c++14", "-O3", "-fopenmp", "-fPIC", "-shared", "-w",
+        # -fno-gnu-unique: both root-count builds are loaded into one process
+        # (ctypes, RTLD_LOCAL); with GNU-unique binding their template static
+        # members (BITPARALLEL_SIZE, which store_index_to_file writes) would
+        # bind process-wide to whichever library was loaded first
+        cmd = ["g++", "-std=c++14", "-O3", "-fopenmp", "-fPIC", "-shared", "-w", "-fno-gnu-unique",
                f"-DPADO_REF_BP_SIZE={k}", "-I", str(REF_INC), "-I", str(ORACLE_DIR),
                str(ORACLE_DIR / "ref_driver.cpp"), "-o", str(out)]
         procs.append((cmd, subprocess.Popen(cmd)))
@@ -136,6 +150,42 @@ def build_reference(force: bool = False, sizes=REF_BP_SIZES) -> list[Path]:
         if p.wait() != 0:
             raise RuntimeError("reference driver build failed: " + " ".join(cmd))
     return outs
+
+
+def vec_so() -> Path:
+    return REF_OUT / "libpado_refvec_k50.so"
+
+
+def host_has_avx512() -> bool:
+    """The reference's AVX-512 classes need an x86 CPU with these extensions."""
+    try:
+        flags = Path("/proc/cpuinfo").read_text()
+    except OSError:
+        return False
+    need = ("avx512f", "avx512bw", "avx512vl", "avx512dq", "avx512cd")
+    return all(f" {x}" in flags for x in need)
+
+
+def build_reference_vec(force: bool = False) -> Path | None:
+    """Compile ref_vec_driver.cpp (the reference's AVX-512 labelers, K = 50)
+    where the staged headers exist and the CPU has AVX-512; else None."""
+    stage_reference()
+    if not host_has_avx512() or not all((REF_INC / h).exists() for h in REF_HEADERS[:2] + REF_VEC_HEADERS):
+        return None
+    out = vec_so()
+    deps = [ORACLE_DIR / "ref_vec_driver.cpp", ORACLE_DIR / "ref_prelude.h", Path(__file__)] + \
+        [REF_INC / h for h in REF_HEADERS[:2] + REF_VEC_HEADERS]
+    if force or not _newer(out, *deps):
+        # -fno-strict-aliasing: the AVX-512 classes read vector lanes through
+        # casted pointers (`int *tmp_vindex = (int *) &vindex;`,
+        # pado_weighted_vec_unp.h:1800), which their intended compiler (icpc)
+        # tolerates; GCC's aliasing optimisation turns those reads into
+        # garbage indices and the weighted class then writes out of bounds
+        cmd = ["g++", "-std=c++14", "-O3", "-fopenmp", "-fPIC", "-shared", "-w", "-fno-gnu-unique",
+               "-fno-strict-aliasing", "-mavx512f", "-mavx512bw", "-mavx512vl", "-mavx512dq", "-mavx512cd", "-DPADO_REF_BP_SIZE=50",
+               "-I", str(REF_INC), "-I", str(ORACLE_DIR), str(ORACLE_DIR / "ref_vec_driver.cpp"), "-o", str(out)]
+        subprocess.run(cmd, check=True)
+    return out
 
 
 REF_TOOLS = {

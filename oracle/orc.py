@@ -219,6 +219,14 @@ def ref(K: int = 50) -> C.CDLL:
         lib.ref_w_query.restype = C.c_double
         lib.ref_w_query.argtypes = [C.c_uint32, _u64p, _u32p, _i16p, C.c_uint64, _u32p, _u32p,
                                     _i16p, C.c_int]
+        lib.ref_unw_store.restype = C.c_int
+        lib.ref_unw_store.argtypes = [C.c_uint32, _u64p, _u32p, _u32p, C.c_uint32, C.c_char_p]
+        lib.ref_w_store.restype = C.c_int
+        lib.ref_w_store.argtypes = [C.c_uint32, _u64p, _u32p, _u8p, _u32p, C.c_uint32, C.c_char_p]
+        lib.ref_unw_load_query.restype = C.c_int64
+        lib.ref_unw_load_query.argtypes = [C.c_char_p, C.c_uint64, _u32p, _u32p, _u8p]
+        lib.ref_w_load_query.restype = C.c_int64
+        lib.ref_w_load_query.argtypes = [C.c_char_p, C.c_uint64, _u32p, _u32p, _i16p]
         lib.ref_graph_read.restype = C.c_void_p
         lib.ref_graph_read.argtypes = [C.c_char_p, C.c_int]
         lib.ref_graph_make.restype = C.c_void_p
@@ -351,6 +359,95 @@ def ref_w_label(g, rank, B: int, mode: int = 0, threads: int = 1) -> WLabels:
     finally:
         lib.ref_w_free(h)
     return WLabels(g.n, off, hub[:tot], dist[:tot], seconds=secs)
+
+
+def ref_unw_store(g, rank, K: int, B: int, path) -> None:
+    """The reference labels g (VertexCentricPLL<B>, K BP roots) and writes
+    its index file with its own store_index_to_file."""
+    lib = ref(K)
+    if lib.ref_unw_store(g.n, _c(g.off, np.uint64), _c(g.adj, np.uint32), _c(rank, np.uint32), B,
+                         str(path).encode()) != 0:
+        raise ValueError(f"reference driver has no batch size {B}")
+
+
+def ref_w_store(g, rank, B: int, path) -> None:
+    """WeightedVertexCentricPLL<B> over g, then its store_index_to_file."""
+    lib = ref(50)
+    if lib.ref_w_store(g.n, _c(g.off, np.uint64), _c(g.adj, np.uint32), _c(g.w, np.uint8), _c(rank, np.uint32), B,
+                       str(path).encode()) != 0:
+        raise ValueError(f"reference driver has no batch size {B}")
+
+
+def ref_load_query(path, a, b, weighted: bool = False, K: int = 50) -> np.ndarray:
+    """The reference's load_index_from_file on `path`, then its
+    query_distance for every pair (query_distance.cpp's loop).  K must be the
+    file's root count (unweighted)."""
+    a, b = _c(a, np.uint32), _c(b, np.uint32)
+    if weighted:
+        out = np.zeros(len(a), np.int16)
+        n = ref(50).ref_w_load_query(str(path).encode(), len(a), a, b, out)
+    else:
+        out = np.zeros(len(a), np.uint8)
+        n = ref(K).ref_unw_load_query(str(path).encode(), len(a), a, b, out)
+    if n < 0:
+        raise ValueError(f"reference loader could not read {path} (missing, or another root count)")
+    return out
+
+
+_refvec = None
+
+
+def refvec_available() -> bool:
+    """The reference's AVX-512 labelers are built (x86 host with AVX-512)."""
+    return _b.vec_so().exists() or _b.build_reference_vec() is not None
+
+
+def refvec() -> C.CDLL:
+    global _refvec
+    if _refvec is None:
+        so = _b.build_reference_vec()
+        if so is None:
+            raise FileNotFoundError("the reference's AVX-512 classes cannot be built on this host")
+        lib = C.CDLL(str(so))
+        lib.refvec_set_threads.argtypes = [C.c_int]
+        lib.refvec_unw_build.restype = C.c_void_p
+        lib.refvec_unw_build.argtypes = [C.c_uint32, _u64p, _u32p, _u32p, C.c_uint32, C.c_int]
+        lib.refvec_w_build.restype = C.c_void_p
+        lib.refvec_w_build.argtypes = [C.c_uint32, _u64p, _u32p, _u8p, _u32p, C.c_uint32, C.c_int]
+        lib.refvec_num_labels.restype = C.c_uint64
+        lib.refvec_num_labels.argtypes = [C.c_void_p]
+        lib.refvec_export.argtypes = [C.c_void_p, _u64p, _u32p, _i16p, C.c_void_p, C.c_void_p]
+        lib.refvec_free.argtypes = [C.c_void_p]
+        _refvec = lib
+    return _refvec
+
+
+def refvec_label(g, rank, B: int, weighted: bool, mode: int = 0, threads: int = 1):
+    """Canonical labels of the reference's AVX-512 class (mode 0 sequential,
+    1 OpenMP; 50 BP roots unweighted).  UnwLabels or WLabels."""
+    lib = refvec()
+    lib.refvec_set_threads(threads)
+    args = (g.n, _c(g.off, np.uint64), _c(g.adj, np.uint32))
+    if weighted:
+        h = lib.refvec_w_build(*args, _c(g.w, np.uint8), _c(rank, np.uint32), B, mode)
+    else:
+        h = lib.refvec_unw_build(*args, _c(rank, np.uint32), B, mode)
+    if not h:
+        raise ValueError(f"no AVX-512 class instance for batch size {B}")
+    try:
+        tot = lib.refvec_num_labels(h)
+        off = np.zeros(g.n + 1, np.uint64)
+        hub = np.zeros(max(tot, 1), np.uint32)
+        dist = np.zeros(max(tot, 1), np.int16)
+        K = 0 if weighted else 50
+        bpd = np.zeros(max(g.n * K, 1), np.uint8)
+        bps = np.zeros(max(g.n * K * 2, 1), np.uint64)
+        lib.refvec_export(h, off, hub, dist, bpd.ctypes.data_as(C.c_void_p), bps.ctypes.data_as(C.c_void_p))
+    finally:
+        lib.refvec_free(h)
+    if weighted:
+        return WLabels(g.n, off, hub[:tot], dist[:tot])
+    return UnwLabels(g.n, K, off, hub[:tot], dist[:tot].astype(np.uint8), bpd[: g.n * K], bps[: g.n * K * 2])
 
 
 def same_unw(a: UnwLabels, b: UnwLabels) -> bool:

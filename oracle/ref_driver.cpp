@@ -199,6 +199,37 @@ WResult *w_run(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8
     return r;
 }
 
+// Labeling followed by the reference's own index writer, as pado.cpp:186-189
+// (unweighted, VertexCentricPLL::store_index_to_file, pado_unw_unv_unp.h:1120-1180)
+// and pado.cpp:270-275 (weighted, WeightedVertexCentricPLL::store_index_to_file,
+// pado_weighted_unv_unp.h:1639-1676) call it: with the original-id -> rank map.
+template <inti B>
+void unw_store(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint32_t *rank, const char *path)
+{
+    Graph G;
+    fill_graph(G, n, off, adj);
+    std::vector<idi> rk(rank, rank + n);
+    G.id_transfer(rk);
+    QuietStdout q;
+    VertexCentricPLL<B> p(G);
+    p.store_index_to_file(path, rk);
+}
+
+template <inti B>
+void w_store(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, const uint32_t *rank,
+             const char *path)
+{
+    WeightedGraph G;
+    fill_graph(G, n, off, adj);
+    G.out_weights = (weighti *)malloc(std::max<size_t>(1, off[n]));
+    for (uint64_t e = 0; e < off[n]; ++e) G.out_weights[e] = w[e];
+    std::vector<idi> rk(rank, rank + n);
+    G.id_transfer(rk);
+    QuietStdout q;
+    WeightedVertexCentricPLL<B> p(G);
+    p.store_index_to_file(path, rk);
+}
+
 // Partial unweighted run for a bounded CPU-baseline sample: the reference's
 // bit-parallel labeling plus its first `nbatches` root batches, called the way
 // ParaVertexCentricPLL::construct() calls them
@@ -295,6 +326,61 @@ double ref_unw_prefix(uint32_t n, const uint64_t *off, const uint32_t *adj, cons
 #undef X
     default: return -1.0;
     }
+}
+
+// The reference's index writers.  0 on success, -1 for an unsupported batch.
+int ref_unw_store(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint32_t *rank, uint32_t B,
+                  const char *path)
+{
+    switch (B) {
+#define X(b) case b: unw_store<b>(n, off, adj, rank, path); return 0;
+        PADO_REF_BATCHES(X)
+#undef X
+    default: return -1;
+    }
+}
+
+int ref_w_store(uint32_t n, const uint64_t *off, const uint32_t *adj, const uint8_t *w, const uint32_t *rank,
+                uint32_t B, const char *path)
+{
+    switch (B) {
+#define X(b) case b: w_store<b>(n, off, adj, w, rank, path); return 0;
+        PADO_REF_BATCHES(X)
+#undef X
+    default: return -1;
+    }
+}
+
+// query_distance.cpp:52-75: the reference's loader (load_index_from_file,
+// pado_unw_unv_unp.h:1182-1224 with the root count read into a local;
+// pado_weighted_unv_unp.h:1678-1711) followed by its query_distance per pair.
+// The unweighted file's root count must equal this build's; returns -1 if it
+// does not (or the file cannot be opened), else the loaded vertex count.
+int64_t ref_unw_load_query(const char *path, uint64_t k, const uint32_t *a, const uint32_t *b, uint8_t *out)
+{
+    uint32_t hdr[2] = {0, 0};
+    FILE *f = fopen(path, "rb");
+    if (!f) return -1;
+    const size_t got = fread(hdr, 4, 2, f);
+    fclose(f);
+    if (got != 2 || hdr[1] != (uint32_t)PADO_REF_BP_SIZE) return -1;
+    QuietStdout q;
+    VertexCentricPLL<1024> p;
+    p.load_index_from_file(path);
+    for (uint64_t i = 0; i < k; ++i) out[i] = p.query_distance(a[i], b[i]);
+    return (int64_t)p.num_v_;
+}
+
+int64_t ref_w_load_query(const char *path, uint64_t k, const uint32_t *a, const uint32_t *b, int16_t *out)
+{
+    FILE *f = fopen(path, "rb");
+    if (!f) return -1;
+    fclose(f);
+    QuietStdout q;
+    WeightedVertexCentricPLL<512> p;
+    p.load_index_from_file(path);
+    for (uint64_t i = 0; i < k; ++i) out[i] = p.query_distance(a[i], b[i]);
+    return (int64_t)p.num_v_;
 }
 
 uint64_t ref_unw_num_labels(void *h) { UnwResult *r = (UnwResult *)h; return r->off[r->n]; }

@@ -27,7 +27,7 @@ sys.path.insert(0, str(REPO))
 from parallel_distance_oracle_gb300 import graphs as G  # noqa: E402
 from oracle import orc  # noqa: E402
 
-REF = Path(os.environ.get("PADO_REFERENCE_DIR", "/root/reference"))
+REF = Path(os.environ.get("PADO_REFERENCE_DIR", REPO.parent / "reference"))
 
 
 def pairs_for(n: int, seed: int, k: int = 1500):
@@ -138,8 +138,49 @@ def _symmetric_weights(g, seed, lo, hi):
     return wu[inv].astype(np.uint8)
 
 
-if __name__ == "__main__" and "--digests" not in sys.argv:
+if __name__ == "__main__" and len(sys.argv) == 1:
     main()
+
+
+# ---------------------------------------------------------------------------
+# Index files written by the reference itself: for a few of the cases above,
+# the reference's sequential labeler (VertexCentricPLL<B> /
+# WeightedVertexCentricPLL<B>) writes its index with store_index_to_file
+# (pado_unw_unv_unp.h:1120-1180, pado_weighted_unv_unp.h:1639-1676), and its
+# load_index_from_file (pado_unw_unv_unp.h:1182-1224 with the root count read
+# into a local; pado_weighted_unv_unp.h:1678-1711) reads the file back and
+# answers the case's query pairs.  Stored: the file's bytes and those answers.
+# Run:  python tests/golden/make_golden.py --index-files
+# ---------------------------------------------------------------------------
+INDEX_FILE_CASES = ["unw_ref_edgelist_k50", "unw_rmat9_k50_b64", "unw_rmat10_k64_b128", "w_ref_weighted_edgelist_b512",
+                    "w_rmat9_w100_b64", "w_rmat10_w7_b128"]
+
+
+def index_files():
+    import tempfile
+    for p in HERE.glob("idxfile_*.npz"):
+        p.unlink()
+    tmp = Path(tempfile.mkdtemp())
+    for case in INDEX_FILE_CASES:
+        z = np.load(HERE / f"{case}.npz")
+        weighted = int(z["kind"]) == 1
+        g = G.CSRGraph(n=int(z["n"]), off=z["off"], adj=z["adj"], w=z["w"] if weighted else None)
+        rank, K, B = z["rank"], int(z["K"]), int(z["B"])
+        path = tmp / f"{case}.idx"
+        if weighted:
+            orc.ref_w_store(g, rank, B, path)
+        else:
+            orc.ref_unw_store(g, rank, K, B, path)
+        loaded = orc.ref_load_query(path, z["qa"], z["qb"], weighted=weighted, K=K)
+        # the reloaded index answers as the labeler's own index does
+        assert np.array_equal(loaded, z["qd"]), f"{case}: reloaded reference index answers differently"
+        raw = np.frombuffer(path.read_bytes(), np.uint8)
+        np.savez_compressed(HERE / f"idxfile_{case}.npz", case=case, raw=raw, qa=z["qa"], qb=z["qb"], qd=loaded)
+        print(f"idxfile_{case}: {len(raw)} bytes")
+
+
+if __name__ == "__main__" and sys.argv[1:2] == ["--index-files"]:
+    index_files()
 
 
 # ---------------------------------------------------------------------------
@@ -191,5 +232,74 @@ def digests():
     (HERE / "full_size_digests.json").write_text(json.dumps(out, indent=1) + "\n")
 
 
-if __name__ == "__main__" and "--digests" in __import__("sys").argv:
+if __name__ == "__main__" and sys.argv[1:2] == ["--digests"]:
     digests()
+
+
+# Query answers and index files at full size, added to the same JSON:
+#   queries -- count, seed and SHA-256 of the answers (uint8 / int16,
+#     little-endian) of the reference's query_distance (pado_unw_unv_unp.h:
+#     1312-1445; weighted pado_weighted_unv_unp.h:1782-1900) over its own
+#     labels, for the workload's query pairs (graphs.random_pairs(n, count,
+#     seed));
+#   index_sha256 / index_bytes -- the file the reference's sequential labeler
+#     writes with its own store_index_to_file (the OpenMP unweighted class's
+#     writer writes nothing: its body is commented out).
+# Run:  python tests/golden/make_golden.py --digests-extra [names...]
+QUERY_SETS = {"rmat14_k50_b1024": (100_000, 11), "rmat20_k64_b1024": (10_000_000, 12), "wrmat18_b512": (1_000_000, 13)}
+
+
+def _sha_file(path):
+    import hashlib
+    h = hashlib.sha256()
+    with open(path, "rb") as f:
+        for chunk in iter(lambda: f.read(1 << 24), b""):
+            h.update(chunk)
+    return h.hexdigest()
+
+
+def digests_extra(names):
+    import hashlib
+    import json
+    import os as _os
+    import tempfile
+    path = HERE / "full_size_digests.json"
+    out = json.loads(path.read_text())
+    threads = _os.cpu_count() or 1
+    for name in names:
+        c = out[name]
+        w = (1, 100) if c["kind"] == "w" else None
+        g = G.rmat(c["scale"], c["ef"], c["seed"], weights=w)
+        rank = G.degree_rank(g)
+        nq, qseed = QUERY_SETS[name]
+        qa, qb = G.random_pairs(g.n, nq, qseed)
+        if c["kind"] == "unw":
+            lab = orc.ref_unw_label(g, rank, c["K"], c["B"], mode=1, threads=threads)
+            assert label_digest("unw", lab.off, lab.hub, lab.dist, lab.bpd, lab.bps) == c["sha256"]
+            ans = np.zeros(nq, np.uint8)
+            orc.ref(c["K"]).ref_unw_query(g.n, lab.off, lab.hub, lab.dist, np.ascontiguousarray(lab.bpd),
+                                          np.ascontiguousarray(lab.bps), nq, qa, qb, ans, threads)
+        else:
+            lab = orc.ref_w_label(g, rank, c["B"], mode=1, threads=threads)
+            assert label_digest("w", lab.off, lab.hub, lab.dist) == c["sha256"]
+            ans = np.zeros(nq, np.int16)
+            orc.ref(50).ref_w_query(g.n, lab.off, lab.hub, lab.dist, nq, qa, qb, ans, threads)
+        del lab
+        c["queries"] = dict(count=nq, seed=qseed, sha256=hashlib.sha256(ans.tobytes()).hexdigest(),
+                            unreachable=int((ans == (255 if c["kind"] == "unw" else 32767)).sum()))
+        print(name, "queries", c["queries"], flush=True)
+        path.write_text(json.dumps(out, indent=1) + "\n")
+        tmp = Path(tempfile.mkdtemp()) / "index.idx"
+        if c["kind"] == "unw":
+            orc.ref_unw_store(g, rank, c["K"], c["B"], tmp)
+        else:
+            orc.ref_w_store(g, rank, c["B"], tmp)
+        c["index_sha256"] = _sha_file(tmp)
+        c["index_bytes"] = tmp.stat().st_size
+        tmp.unlink()
+        print(name, "index", c["index_sha256"], c["index_bytes"], flush=True)
+        path.write_text(json.dumps(out, indent=1) + "\n")
+
+
+if __name__ == "__main__" and sys.argv[1:2] == ["--digests-extra"]:
+    digests_extra([a for a in sys.argv[2:] if not a.startswith("-")] or list(QUERY_SETS))

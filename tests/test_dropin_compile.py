@@ -1,14 +1,14 @@
 """The drop-in header compiles with the drivers: our own driver (always) and,
 where the reference tree is available, the reference's unmodified pado.cpp and
 query_distance.cpp with their labeler headers mapped to include/pado_gpu.hpp."""
-import os
-from pathlib import Path
 
 import pytest
 
 from dropin.build_dropin import build
 
-REF = Path(os.environ.get("PADO_REFERENCE_DIR", "/root/reference"))
+from oracle.build_oracle import _reference_dir
+
+REF = _reference_dir()
 LABELER_HEADERS = [
     "pado_unw_unv_para.201912311607.parallel_bp_labeling.h", "pado_unw_unv_unp.h", "pado_unw_vec_unp.h",
     "pado_unw_vec_para.h", "pado_weighted_unv_unp.h", "pado_weighted_vec_unp.h", "pado_weighted_unv_para.h",
