@@ -9,8 +9,9 @@ compiled reference made (tests/golden/make_golden.py --digests and
 * queries: the GPU's answers to the workload's own query pairs (100k, 10M and
   1M uniform pairs, seeds 11 / 12 / 13) hash to the SHA-256 of the reference's
   query_distance answers over its own labels (pado_unw_unv_unp.h:1312-1445,
-  pado_weighted_unv_unp.h:1782-1900), and 2,000 of those pairs, grouped under
-  20 sources, equal a plain BFS / Dijkstra from the source;
+  pado_weighted_unv_unp.h:1782-1900), and 2,000 pairs under 20 of those
+  sources equal a plain BFS / Dijkstra from the source, except where the
+  reference's own query skips a bit-parallel root (see below);
 * index file: pado_store writes the same bytes as the reference's
   store_index_to_file on the same labeling (digest of the whole file)."""
 import hashlib
@@ -82,14 +83,24 @@ def test_full_size_queries_match_reference_and_bfs(built):
     ans = idx.query(qa, qb)
     assert ans.dtype == (np.uint8 if c["kind"] == "unw" else np.int16)
     assert hashlib.sha256(np.ascontiguousarray(ans).tobytes()).hexdigest() == q["sha256"]
-    # 20 sources (the first pair endpoints), 100 targets each
+    # 20 sources (the first pair endpoints), 100 targets each, against BFS /
+    # Dijkstra.  One documented exception, the reference's own: its query
+    # compares `int td - 2` with an unsigned bound (pado_unw_unv_unp.h:1345),
+    # so a bit-parallel root whose two BP distances sum to less than 2 (the
+    # root itself and one of its chosen neighbours) is skipped, and such an
+    # adjacent pair can come out longer than 1.  The GPU reproduces the
+    # reference's answer there (the digest above covers it).
+    K = int(c["K"])
+    bpd = idx.export().bpd.reshape(g.n, K) if K else None
     rng = np.random.Generator(np.random.PCG64(q["seed"] + 1000))
     for s in qa[:20]:
         tg = rng.integers(0, g.n, 100).astype(np.uint32)
-        src = np.full(100, s, np.uint32)
-        got = idx.query(src, tg)
-        truth = orc.bfs(g, int(s)) if c["kind"] == "unw" else orc.dijkstra(g, int(s))
-        assert np.array_equal(got.astype(np.int64), truth[tg].astype(np.int64)), f"{name}: source {s}"
+        got = idx.query(np.full(100, s, np.uint32), tg).astype(np.int64)
+        truth = (orc.bfs(g, int(s)) if c["kind"] == "unw" else orc.dijkstra(g, int(s)))[tg].astype(np.int64)
+        for i in np.nonzero(got != truth)[0]:
+            assert K and got[i] > truth[i], f"{name}: source {s} target {tg[i]}"
+            sums = bpd[s].astype(np.int64) + bpd[tg[i]].astype(np.int64)
+            assert (sums < 2).any(), f"{name}: source {s} target {tg[i]}: not the skipped-root case"
 
 
 def test_full_size_index_file_matches_reference(built, tmp_path):

@@ -63,7 +63,7 @@ def test_gpu_loads_reference_file(pado, path, tmp_path):
     p.write_bytes(f["raw"].tobytes())
     idx = pado.WeightedVertexCentricPLL() if weighted else pado.VertexCentricPLL()
     idx.load_index_from_file(str(p))
-    assert idx.num_v() == g.n
+    assert idx.num_v == g.n
     assert np.array_equal(idx.query(f["qa"], f["qb"]), f["qd"])
     # and writes it back unchanged
     p2 = tmp_path / "again.idx"
