@@ -335,58 +335,61 @@ __device__ __forceinline__ bool bp_one(uint8_t rd, ulonglong2 rs, uint8_t td, ul
 
 // Warp-cooperative BP test of candidate root r against the tail's row held in
 // registers (lane i holds BP roots i and i + 32); roots < skip were already
-// tested.  Pruned iff any root covers the pair -- order-independent.
+// tested.  Pruned iff any root covers the pair -- order-independent.  The
+// candidate's distances and sets are loaded in one round.
 __device__ __forceinline__ bool bp_covered_warp(const UnwDev &d, uint32_t r, int lane, uint32_t skip, uint8_t td0,
                                                 ulonglong2 ts0, uint8_t td1, ulonglong2 ts1, uint32_t iter)
 {
     const uint8_t *rd = d.bpd + (uint64_t)r * d.K;
     const ulonglong2 *rs = reinterpret_cast<const ulonglong2 *>(d.bps + (uint64_t)r * d.K * 2);
-    bool cov = false;
     const uint32_t i0 = lane, i1 = lane + 32;
-    if (i0 >= skip && i0 < d.K) cov = bp_one(rd[i0], rs[i0], td0, ts0, iter);
-    if (i1 >= skip && i1 < d.K) cov = cov || bp_one(rd[i1], rs[i1], td1, ts1, iter);
+    const bool v0 = i0 >= skip && i0 < d.K, v1 = i1 >= skip && i1 < d.K;
+    const ulonglong2 z = make_ulonglong2(0, 0);
+    const uint8_t a0 = v0 ? rd[i0] : (uint8_t)U8_INF, a1 = v1 ? rd[i1] : (uint8_t)U8_INF;
+    const ulonglong2 s0 = v0 ? rs[i0] : z, s1 = v1 ? rs[i1] : z;
+    const bool cov = (v0 && bp_one(a0, s0, td0, ts0, iter)) || (v1 && bp_one(a1, s1, td1, ts1, iter));
     return __ballot_sync(FULL, cov) != 0;
 }
 
 // Warp-cooperative BP test of up to BP_GROUP candidates at once (the first
-// `nc` of r[]), distances first: every candidate's distances are loaded in one
-// round, then a root's 16-byte sets only where its distance sum can prune
-// (x - 2 <= iter), in a second round -- sparse graphs, where BP distances are
-// mostly too large, read 64 bytes per candidate instead of 1 KB.  Bit c of the
-// result: r[c] covered.
-constexpr int BP_GROUP = 2;
+// `nc` of r[]): each candidate's distances and the 16-byte sets of lane i's
+// two roots are loaded in one round (1 KB per candidate at K = 64), then
+// tested.  On social graphs nearly every pair that reaches this stage needs
+// most roots' sets, so loading them with the distances saves a round trip per
+// candidate; one candidate per step keeps the loop kernel free of register
+// spills.  Bit c of the result: r[c] covered.
+constexpr int BP_GROUP = 1;
 __device__ __forceinline__ uint32_t bp_covered_group(const UnwDev &d, const uint32_t (&r)[BP_GROUP], uint32_t nc,
                                                      int lane, uint32_t skip, uint8_t td0, ulonglong2 ts0, uint8_t td1,
                                                      ulonglong2 ts1, uint32_t iter)
 {
     const uint32_t K = d.K, i0 = lane, i1 = lane + 32;
     const bool v0 = i0 >= skip && i0 < K, v1 = i1 >= skip && i1 < K;
+    const ulonglong2 z = make_ulonglong2(0, 0);
     uint32_t x0[BP_GROUP], x1[BP_GROUP];
+    ulonglong2 s0[BP_GROUP], s1[BP_GROUP];
 #pragma unroll
     for (int c = 0; c < BP_GROUP; ++c) {
+        const bool in = (uint32_t)c < nc;
         const uint8_t *rd = d.bpd + (uint64_t)r[c] * K;
-        x0[c] = (uint32_t)c < nc && v0 ? (uint32_t)rd[i0] + td0 : 0u;  // 0: fails the test like x < 2 does
-        x1[c] = (uint32_t)c < nc && v1 ? (uint32_t)rd[i1] + td1 : 0u;
+        const ulonglong2 *rs = reinterpret_cast<const ulonglong2 *>(d.bps) + (uint64_t)r[c] * K;
+        x0[c] = in && v0 ? (uint32_t)rd[i0] + td0 : 0u;  // 0: fails the test like x < 2 does
+        x1[c] = in && v1 ? (uint32_t)rd[i1] + td1 : 0u;
+        s0[c] = in && v0 ? rs[i0] : z;
+        s1[c] = in && v1 ? rs[i1] : z;
     }
     auto cut = [&](uint32_t x, ulonglong2 rs, ulonglong2 ts) {
+        if (x - 2u > iter) return false;
         if (rs.x & ts.x)
             x -= 2u;
         else if ((rs.x & ts.y) | (rs.y & ts.x))
             x -= 1u;
         return x <= iter;
     };
-    bool cov[BP_GROUP];
-#pragma unroll
-    for (int c = 0; c < BP_GROUP; ++c) {
-        const ulonglong2 *rs = reinterpret_cast<const ulonglong2 *>(d.bps) + (uint64_t)r[c] * K;
-        cov[c] = false;
-        if (x0[c] - 2u <= iter) cov[c] = cut(x0[c], rs[i0], ts0);
-        if (x1[c] - 2u <= iter) cov[c] = cov[c] || cut(x1[c], rs[i1], ts1);
-    }
     uint32_t res = 0;
 #pragma unroll
     for (int c = 0; c < BP_GROUP; ++c)
-        if (__ballot_sync(FULL, cov[c])) res |= 1u << c;
+        if (__ballot_sync(FULL, cut(x0[c], s0[c], ts0) || cut(x1[c], s1[c], ts1))) res |= 1u << c;
     return res;
 }
 
