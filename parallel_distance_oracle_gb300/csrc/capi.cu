@@ -1049,6 +1049,7 @@ int pado_export(const pado_index *h, uint64_t *off, uint32_t *hub, void *dist, u
     if (!h || !off || (h->store.total && (!hub || !dist))) return fail(PADO_E_ARG, "null argument");
     if (h->offloaded) return fail(PADO_E_STATE, "index is offloaded to host memory by a serving loop");
     return guarded([&] {
+        pado::HostPhase ph("export");
         PADO_CUDA(cudaSetDevice(h->device));
         const uint32_t n = h->n, K = h->K;
         const uint64_t tot = h->store.total;

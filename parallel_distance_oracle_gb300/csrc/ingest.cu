@@ -983,13 +983,15 @@ DevGraph prepare_csr(uint32_t n, const uint64_t *off, const uint32_t *adj, const
     DevGraph g;
     g.n = n;
     g.m = m;
-    g.off.alloc((uint64_t)n + 1);
-    g.adj.alloc(std::max<uint64_t>(m, 1));
-    g.adj.upload(adj, m, s);
-    if (w) {
-        g.w.alloc(std::max<uint64_t>(m, 1));
-        g.w.upload(w, m, s);
+    {
+        HostPhase ph("csr alloc");
+        g.off.alloc((uint64_t)n + 1);
+        g.adj.alloc(std::max<uint64_t>(m, 1));
+        if (w) g.w.alloc(std::max<uint64_t>(m, 1));
     }
+    HostPhase ph("csr upload+check");
+    g.adj.upload(adj, m, s);
+    if (w) g.w.upload(w, m, s);
     PBuf<uint64_t> off64((uint64_t)n + 1, s);
     PADO_CUDA(cudaMemcpyAsync(off64.p, off, ((uint64_t)n + 1) * 8, cudaMemcpyHostToDevice, s));
     PBuf<uint32_t> flags(1, s);

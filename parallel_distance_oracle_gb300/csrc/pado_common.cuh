@@ -4,7 +4,10 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -39,6 +42,25 @@ struct Error : std::runtime_error {
     do {                                                             \
         if (!(cond)) throw ::pado::Error((code), (msg));             \
     } while (0)
+
+// A host-side phase of a library call: an NVTX range (shown by Nsight tools
+// when one is attached; a no-op otherwise) and, with PADO_TRACE set in the
+// environment, the phase's wall time on stderr when it ends.
+struct HostPhase {
+    const char *name;
+    std::chrono::steady_clock::time_point t0;
+    explicit HostPhase(const char *n) : name(n), t0(std::chrono::steady_clock::now()) { nvtxRangePushA(n); }
+    HostPhase(const HostPhase &) = delete;
+    HostPhase &operator=(const HostPhase &) = delete;
+    ~HostPhase()
+    {
+        nvtxRangePop();
+        static const bool trace = std::getenv("PADO_TRACE") != nullptr;
+        if (trace)
+            fprintf(stderr, "phase %s %.3f ms\n", name,
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+    }
+};
 
 // Owning device buffer.
 template <typename T>

@@ -47,6 +47,7 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <optional>
 
 #include "unw_device.cuh"
 
@@ -299,6 +300,9 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     const uint32_t words = (B + 31) / 32;
     PADO_CHECK(B >= 1 && B <= MAX_BATCH, PADO_E_ARG, "batch size must be in [1, 2048]");
     PADO_CHECK(K <= MAX_BP, PADO_E_ARG, "at most 64 bit-parallel roots");
+    // destroyed after every buffer below: times their release
+    std::optional<HostPhase> release_phase;
+    std::optional<HostPhase> alloc_phase(std::in_place, "label alloc");
 
     DBuf<uint8_t> d_used(std::max<uint32_t>(n, 1));
     d_used.upload(used.data(), n, s);
@@ -397,6 +401,8 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     cudaEvent_t e0, e1;
     PADO_CUDA(cudaEventCreate(&e0));
     PADO_CUDA(cudaEventCreate(&e1));
+    alloc_phase.reset();
+    std::optional<HostPhase> loop_phase(std::in_place, "label loop");
     PADO_CUDA(cudaEventRecord(e0, s));
     uint32_t lid = 0;
     std::vector<uint32_t> hroots;
@@ -525,6 +531,7 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
                 if (!used[r]) hroots.push_back(r);
             ++run.batches;
             if (hroots.empty()) continue;
+            nvtxRangePushA("batch");
             const uint32_t nr = (uint32_t)hroots.size();
             roots.upload(hroots.data(), nr, s);
             const uint32_t lid0 = ++lid;
@@ -555,6 +562,7 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
                     throw Error(PADO_E_OVERFLOW, "BFS level reached 255 (uint8 distance overflow)");
                 const uint32_t lid_cur = ++lid;
                 const int nxt = cur ^ 1;
+                nvtxRangePushA("level");
                 PADO_CUDA(cudaMemsetAsync(c_tails, 0, 4, s));
                 PADO_CUDA(cudaMemsetAsync(c_htails, 0, 4, s));
                 PADO_CUDA(cudaMemsetAsync(c_front[nxt], 0, 4, s));
@@ -587,6 +595,7 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
                 }
                 fsize = hc->front_next;
                 cur = nxt;
+                nvtxRangePop();
             }
             PADO_LAUNCH("dm_rows_kernel(reset)", s,
                         dm_rows_kernel<<<grid_for((uint64_t)nr * 32, 256), 256, 0, s>>>(d, roots.p, nr, bs, 0));
@@ -596,6 +605,7 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
                 PADO_CUDA(cudaEventRecord(tr.ev, s));
                 trace_rows.push_back(tr);
             }
+            nvtxRangePop();
         }
         if (trace) {
             PADO_CUDA(cudaStreamSynchronize(s));
@@ -611,6 +621,8 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
             if (prev != e0) cudaEventDestroy(prev);
         }
         // finalize: exact-size canonical store
+        loop_phase.reset();
+        HostPhase fin_phase("label finalize");
         std::vector<uint32_t> lens(n);
         lab_len.download(lens.data(), n, s);
         PADO_CUDA(cudaStreamSynchronize(s));
@@ -637,6 +649,7 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFreeHost(hc);
+    release_phase.emplace("label release");
     return run;
 }
 
