@@ -12,15 +12,22 @@
 //     from a library either fails or breaks the owner's accounting.
 // For them pado_query_noalloc() stages through one fixed area that is part of
 // the library image: a file-scope __device__ array of NOALLOC_MAX_PAIRS pairs
-// (2.5 MiB), present on every GPU that loads the library until the process
-// exits.  Host code cannot use the array's name as a device address, so the
-// first call on each device looks its address up with cudaGetSymbolAddress
-// while that device is current and remembers it; that first call should
-// happen before any stream capture.  Nothing in the area needs to start at
-// zero: every call writes the slots it reads.  All calls on a device share the
-// area and keep the last call's contents, so calls that overlap on the GPU
-// (for example from two host threads at once) race on it; callers must
-// serialise them.
+// (2.5 MiB), held on every GPU where the library's device code is loaded
+// until the process exits.  Host code cannot use the array's name as a device
+// address, so the first call on each device looks its address up with
+// cudaGetSymbolAddress while that device is current and remembers it; that
+// first call should happen before any stream capture, and it is the slow one:
+// with lazy module loading (the default since CUDA 12.2) it is also what loads
+// the library's device code and creates the area, which the driver may do
+// with allocations and synchronisation of its own.  Callers make one warm-up
+// call per device (k >= 1) before their latency-sensitive section.  A device
+// reset (cudaDeviceReset) unloads the area; the remembered address is stale
+// afterwards, so this entry point must not be used on a device after it was
+// reset.  Nothing in the area needs to start at zero: every call writes the
+// slots it reads.  All calls on a device share the area and keep the last
+// call's contents, so calls that overlap on the GPU (for example from two host
+// threads at once) race on it; callers must serialise them.  The caller's
+// current device is left as it was.
 
 #include <map>
 #include <mutex>
@@ -72,33 +79,47 @@ int pado_query_noalloc(pado_index *h, uint64_t k, const uint32_t *a, const uint3
     if (!k) return PADO_OK;
     if (!pado::index_resident(h))
         return pado::set_error(PADO_E_STATE, "index is offloaded to host memory by a serving loop");
+    int prev = -1;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e != cudaSuccess) return pado::set_error(PADO_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     const int dev = pado::index_device(h);
-    cudaError_t e = cudaSetDevice(dev);
-    if (e != cudaSuccess) return pado::set_error(PADO_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
-    unsigned char *base = nullptr;
-    int st = scratch_on_device(dev, &base);
-    if (st != PADO_OK) return st;
-    uint32_t *da = reinterpret_cast<uint32_t *>(base);
-    uint32_t *db = reinterpret_cast<uint32_t *>(base + NOALLOC_MAX_PAIRS * 4);
-    unsigned char *dout = base + NOALLOC_MAX_PAIRS * 8;
-    const bool unw = pado::index_kind(h) == PADO_UNWEIGHTED;
-    const size_t osz = unw ? 1 : 2;
+    if (dev != prev) {
+        e = cudaSetDevice(dev);
+        if (e != cudaSuccess)
+            return pado::set_error(PADO_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    }
     cudaStream_t s = cudaStreamPerThread;
+    int st = PADO_OK;
     try {
-        PADO_CUDA(cudaMemcpyAsync(da, a, k * 4, cudaMemcpyHostToDevice, s));
-        PADO_CUDA(cudaMemcpyAsync(db, b, k * 4, cudaMemcpyHostToDevice, s));
-        const pado::IndexView v = pado::index_view(h);
-        if (unw)
-            pado::launch_query_unw(v, k, da, db, dout, s);
-        else
-            pado::launch_query_w(v, k, da, db, reinterpret_cast<int16_t *>(dout), s);
-        PADO_CUDA(cudaMemcpyAsync(out, dout, k * osz, cudaMemcpyDeviceToHost, s));
-        PADO_CUDA(cudaStreamSynchronize(s));
+        unsigned char *base = nullptr;
+        st = scratch_on_device(dev, &base);
+        if (st == PADO_OK) {
+            uint32_t *da = reinterpret_cast<uint32_t *>(base);
+            uint32_t *db = reinterpret_cast<uint32_t *>(base + NOALLOC_MAX_PAIRS * 4);
+            unsigned char *dout = base + NOALLOC_MAX_PAIRS * 8;
+            const bool unw = pado::index_kind(h) == PADO_UNWEIGHTED;
+            const size_t osz = unw ? 1 : 2;
+            PADO_CUDA(cudaMemcpyAsync(da, a, k * 4, cudaMemcpyHostToDevice, s));
+            PADO_CUDA(cudaMemcpyAsync(db, b, k * 4, cudaMemcpyHostToDevice, s));
+            const pado::IndexView v = pado::index_view(h);
+            if (unw)
+                pado::launch_query_unw(v, k, da, db, dout, s);
+            else
+                pado::launch_query_w(v, k, da, db, reinterpret_cast<int16_t *>(dout), s);
+            PADO_CUDA(cudaMemcpyAsync(out, dout, k * osz, cudaMemcpyDeviceToHost, s));
+            PADO_CUDA(cudaStreamSynchronize(s));
+        }
     } catch (const pado::Error &err) {
         cudaStreamSynchronize(s);
-        return pado::set_error(err.code, err.what());
+        st = pado::set_error(err.code, err.what());
+    } catch (const std::bad_alloc &) {
+        st = pado::set_error(PADO_E_NOMEM, "host allocation failed");
+    } catch (const std::exception &err) {
+        cudaStreamSynchronize(s);
+        st = pado::set_error(PADO_E_CUDA, err.what());
     }
-    return PADO_OK;
+    if (dev != prev) cudaSetDevice(prev);
+    return st;
 }
 
 }  // extern "C"

@@ -10,6 +10,12 @@ This file is named to be collected last, so a run that stops at the first
 failure has run every other test already; it also passes on its own.
 """
 import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import textwrap
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -76,3 +82,81 @@ def test_noalloc_rejects_batches_beyond_its_area(lib):
     a, b = _pairs(g.n, 1000, 4)
     assert np.array_equal(_query(lib, idx._h, "pado_query_noalloc", a, b, np.uint8),
                           _query(lib, idx._h, "pado_query", a, b, np.uint8))
+
+
+# A preloaded stand-in for the CUDA runtime's allocation calls: each call is
+# counted, then forwarded to the runtime the library loaded.  The library
+# reaches the runtime through its shared object (libcudart.so.13), so these
+# definitions interpose on every allocation or free it makes.
+SHIM = r"""
+#define _GNU_SOURCE
+#include <dlfcn.h>
+#include <stddef.h>
+static long g_calls;
+long shim_alloc_calls(void) { return g_calls; }
+static void *real_sym(const char *name)
+{
+    void *h = dlopen("libcudart.so.13", RTLD_LAZY | RTLD_NOLOAD);
+    return h ? dlsym(h, name) : NULL;
+}
+#define WRAP(name, params, args) \
+    int name params { static int (*real) params; if (!real) real = (int (*) params)real_sym(#name); \
+                      ++g_calls; return real ? real args : 999; }
+WRAP(cudaMalloc, (void **p, size_t n), (p, n))
+WRAP(cudaMallocAsync, (void **p, size_t n, void *s), (p, n, s))
+WRAP(cudaMallocFromPoolAsync, (void **p, size_t n, void *pool, void *s), (p, n, pool, s))
+WRAP(cudaMallocManaged, (void **p, size_t n, unsigned f), (p, n, f))
+WRAP(cudaMallocPitch, (void **p, size_t *pitch, size_t w, size_t h), (p, pitch, w, h))
+WRAP(cudaMallocHost, (void **p, size_t n), (p, n))
+WRAP(cudaHostAlloc, (void **p, size_t n, unsigned f), (p, n, f))
+WRAP(cudaFree, (void *p), (p))
+WRAP(cudaFreeAsync, (void *p, void *s), (p, s))
+WRAP(cudaFreeHost, (void *p), (p))
+"""
+
+CHILD = r"""
+import ctypes as C, json, sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+from parallel_distance_oracle_gb300 import graphs as G, pado, _lib
+calls = C.CDLL(None).shim_alloc_calls
+calls.restype = C.c_long
+g = G.rmat(12, 8, 43)
+idx = pado.VertexCentricPLL(g, G.degree_rank(g), bp_roots=50, batch=512)
+ptr = lambda x: x.ctypes.data_as(C.c_void_p)
+def q(fn, a, b):
+    out = np.full(len(a), 77, np.uint8)
+    st = getattr(_lib.lib, fn)(idx._h, len(a), ptr(a), ptr(b), ptr(out))
+    return st, out
+a1, b1 = (np.ascontiguousarray(x) for x in G.random_pairs(g.n, 262144, 7, distinct=False))
+a2, b2 = (np.ascontiguousarray(x) for x in G.random_pairs(g.n, 3000, 8, distinct=False))
+warm, _ = q("pado_query_noalloc", a2, b2)      # first call on the device: set-up
+c0 = calls()
+s1, o1 = q("pado_query_noalloc", a1, b1)
+s2, o2 = q("pado_query_noalloc", a2, b2)
+c1 = calls()
+s3, w1 = q("pado_query", a1, b1)                # the allocating entry point, for contrast
+c2 = calls()
+print(json.dumps(dict(warm=warm, s1=s1, s2=s2, s3=s3, noalloc_calls=c1 - c0, query_calls=c2 - c1,
+                      same=bool(np.array_equal(o1, w1)))))
+"""
+
+
+def test_noalloc_makes_no_allocation_calls(lib, tmp_path):
+    """Two calls after the warm-up make no allocation or free call into the
+    CUDA runtime (counted by a preloaded stand-in in a child process), while
+    pado_query on the same pairs does -- the count sees this library's calls."""
+    shim_c, shim = tmp_path / "shim.c", tmp_path / "shim.so"
+    shim_c.write_text(SHIM)
+    subprocess.run(["gcc", "-shared", "-fPIC", "-O2", "-o", str(shim), str(shim_c), "-ldl"], check=True)
+    child = tmp_path / "child.py"
+    child.write_text(textwrap.dedent(CHILD))
+    repo = str(Path(__file__).resolve().parents[1])
+    env = dict(os.environ, LD_PRELOAD=str(shim))
+    r = subprocess.run([sys.executable, str(child), repo], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert res["warm"] == 0 and res["s1"] == 0 and res["s2"] == 0 and res["s3"] == 0, res
+    assert res["same"], res
+    assert res["noalloc_calls"] == 0, res
+    assert res["query_calls"] > 0, res
