@@ -309,12 +309,18 @@ int pado_load(const char *path, uint32_t kind, pado_index **out);
  * device memory -- latency-bound serving threads, where cudaMalloc/cudaFree can
  * block on device-wide synchronisation, and processes whose GPU memory is owned
  * by another allocator: the pairs and results are staged through a fixed
- * 2.5 MiB area compiled into the library (present on every GPU that loads it),
- * so at most PADO_NOALLOC_MAX_PAIRS pairs per call (more -> PADO_E_ARG).
- * Same arguments and results as pado_query; synchronous.  The first call on a
- * device looks the area's address up (do it before any stream capture).  All
- * calls on a device share the area: calls that overlap on the GPU (e.g. from
- * two host threads at once) race on it and must be serialised by the caller.
+ * 2.5 MiB area compiled into the library, so at most PADO_NOALLOC_MAX_PAIRS
+ * pairs per call (more -> PADO_E_ARG).  Same arguments and results as
+ * pado_query; synchronous; the caller's current device is left as it was.
+ * The first call on a device is the slow one: it looks the area's address up,
+ * and with lazy module loading (the CUDA default) it is what loads the
+ * library's device code and so creates the area.  Make one warm-up call per
+ * device (k >= 1) before any latency-sensitive section and before any stream
+ * capture.  After a device reset (cudaDeviceReset) the area is gone and the
+ * address this library remembered is stale: do not use this entry point on a
+ * device that was reset.  All calls on a device share the area: calls that
+ * overlap on the GPU (e.g. from two host threads at once) race on it and must
+ * be serialised by the caller.
  * ------------------------------------------------------------------------- */
 #define PADO_NOALLOC_MAX_PAIRS 262144u
 int pado_query_noalloc(pado_index *h, uint64_t k, const uint32_t *a, const uint32_t *b, void *out);
@@ -325,6 +331,25 @@ int pado_query_noalloc(pado_index *h, uint64_t k, const uint32_t *a, const uint3
  * ------------------------------------------------------------------------- */
 /* Kernel launches this library has made in the process so far. */
 uint64_t pado_kernel_launches(void);
+
+/* ---------------------------------------------------------------------------
+ * Failure detection, for tests (no counterpart in the reference, which exits
+ * on I/O errors and has no device code).  None of them faults or hangs a GPU.
+ * ------------------------------------------------------------------------- */
+/* Make the nth device allocation of this library from now on (1 = the next)
+ * fail as if the device were out of memory: the call that makes it returns
+ * PADO_E_NOMEM and releases what it had allocated.  0 disarms. */
+int pado_debug_fail_alloc(uint64_t nth);
+/* Device buffers of this library currently allocated (indexes, servers and
+ * scratch in use); a failed call leaves it where it was. */
+int64_t pado_debug_live_allocations(void);
+/* Runs the labeling loops' bounded grid barrier in a cooperative launch of
+ * `blocks` blocks (1..152) in which block `absent_block` never arrives
+ * (absent_block >= blocks: all arrive), each waiting block giving up after
+ * timeout_ns (at most 1 s).  Returns PADO_E_TIMEOUT when the wait ran out,
+ * PADO_OK when the barrier completed; *blocks_returned counts the blocks that
+ * returned (all of them, either way). */
+int pado_selftest_barrier(uint32_t blocks, uint32_t absent_block, uint64_t timeout_ns, uint32_t *blocks_returned);
 
 /* ---------------------------------------------------------------------------
  * Serving loop (continuous batching).  The reference answers pairs one call

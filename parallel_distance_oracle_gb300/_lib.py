@@ -80,6 +80,9 @@ def _load() -> C.CDLL:
         "pado_load": (C.c_int, [C.c_char_p, u32, P(vp)]),
         "pado_query_noalloc": (C.c_int, [vp, u64, vp, vp, vp]),
         "pado_kernel_launches": (u64, []),
+        "pado_debug_fail_alloc": (C.c_int, [u64]),
+        "pado_debug_live_allocations": (C.c_int64, []),
+        "pado_selftest_barrier": (C.c_int, [u32, u32, u64, P(u32)]),
         "pado_server_create": (C.c_int, [u64, u32, u32, P(vp)]),
         "pado_server_add": (C.c_int, [vp, vp, P(u32)]),
         "pado_server_submit": (C.c_int, [vp, u32, u64, vp, vp, vp, P(u64)]),
@@ -109,7 +112,8 @@ EXPORTED = [
     "pado_unw_build_edges", "pado_w_build_edges",
     "pado_build_edge_file", "pado_edge_text_parse", "pado_set_order", "pado_free", "pado_get_info", "pado_export",
     "pado_import", "pado_query", "pado_query_device", "pado_query_noalloc", "pado_store", "pado_load",
-    "pado_kernel_launches", "pado_server_create", "pado_server_add", "pado_server_submit", "pado_server_wait",
+    "pado_kernel_launches", "pado_debug_fail_alloc", "pado_debug_live_allocations", "pado_selftest_barrier",
+    "pado_server_create", "pado_server_add", "pado_server_submit", "pado_server_wait",
     "pado_server_get_stats", "pado_server_replay", "pado_server_destroy",
     "pado_profile", "pado_profile_read",
 ]

@@ -21,7 +21,7 @@ INCLUDE = REPO / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libpado_gpu.so"
 SOURCES = ["capi.cu", "query.cu", "bp.cu", "unw.cu", "unw_many.cu", "weighted.cu", "profile.cu", "noalloc.cu",
-           "serve.cu", "ingest.cu"]
+           "serve.cu", "ingest.cu", "selftest.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

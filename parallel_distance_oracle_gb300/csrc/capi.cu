@@ -1023,9 +1023,12 @@ int pado_set_order(pado_index *h, const uint32_t *rank)
     return guarded([&] {
         check_rank(h->n, rank);
         PADO_CUDA(cudaSetDevice(h->device));
+        // the calling thread's stream: other streams of the device (a serving
+        // loop's, say) keep running
+        const cudaStream_t s = cudaStreamPerThread;
         h->rank.alloc(std::max<uint32_t>(h->n, 1));
-        h->rank.upload(rank, h->n, 0);
-        PADO_CUDA(cudaDeviceSynchronize());
+        h->rank.upload(rank, h->n, s);
+        PADO_CUDA(cudaStreamSynchronize(s));
         h->info.device_bytes = h->device_bytes();
     });
 }
@@ -1130,23 +1133,23 @@ int pado_import(uint32_t kind, uint32_t n, uint32_t bp_roots, const uint64_t *of
         h->K = bp_roots;
         h->store.total = tot;
         h->store.off.alloc(n + 1);
-        h->store.off.upload(off, n + 1);
+        h->store.off.upload(off, n + 1, cudaStreamPerThread);
         h->store.hub.alloc(std::max<uint64_t>(tot, 1));
-        h->store.hub.upload(hub, tot);
+        h->store.hub.upload(hub, tot, cudaStreamPerThread);
         if (kind == PADO_UNWEIGHTED) {
             h->store.dist8.alloc(std::max<uint64_t>(tot, 1));
-            h->store.dist8.upload(static_cast<const uint8_t *>(dist), tot);
+            h->store.dist8.upload(static_cast<const uint8_t *>(dist), tot, cudaStreamPerThread);
         } else {
             h->store.dist16.alloc(std::max<uint64_t>(tot, 1));
-            h->store.dist16.upload(static_cast<const int16_t *>(dist), tot);
+            h->store.dist16.upload(static_cast<const int16_t *>(dist), tot, cudaStreamPerThread);
         }
         if (bp_roots) {
             h->bpd.alloc((uint64_t)n * bp_roots);
-            h->bpd.upload(bp_dist, (uint64_t)n * bp_roots);
+            h->bpd.upload(bp_dist, (uint64_t)n * bp_roots, cudaStreamPerThread);
             h->bps.alloc((uint64_t)n * bp_roots * 2);
-            h->bps.upload(bp_sets, (uint64_t)n * bp_roots * 2);
+            h->bps.upload(bp_sets, (uint64_t)n * bp_roots * 2, cudaStreamPerThread);
         }
-        PADO_CUDA(cudaDeviceSynchronize());
+        PADO_CUDA(cudaStreamSynchronize(cudaStreamPerThread));  // this thread's stream only
         h->info.n = n;
         h->info.kind = kind;
         h->info.bp_roots = bp_roots;

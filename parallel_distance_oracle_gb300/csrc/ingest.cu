@@ -170,13 +170,20 @@ struct PBuf {
     cudaStream_t s = nullptr;
     PBuf(size_t count, cudaStream_t st) : n(count), s(st)
     {
-        if (count) PADO_CUDA(cudaMallocFromPoolAsync((void **)&p, count * sizeof(T), scratch_pool(), s));
+        if (count) {
+            alloc_point();
+            PADO_CUDA(cudaMallocFromPoolAsync((void **)&p, count * sizeof(T), scratch_pool(), s));
+            alloc_live(1);
+        }
     }
     PBuf(const PBuf &) = delete;
     PBuf &operator=(const PBuf &) = delete;
     ~PBuf()
     {
-        if (p) cudaFreeAsync(p, s);
+        if (p) {
+            cudaFreeAsync(p, s);
+            alloc_live(-1);
+        }
     }
     void zero()
     {

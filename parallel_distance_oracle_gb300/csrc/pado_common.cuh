@@ -62,6 +62,13 @@ struct HostPhase {
     }
 };
 
+// Allocation accounting (profile.cu): every device buffer of the library
+// passes alloc_point() before it allocates -- which fails the allocation
+// with PADO_E_NOMEM when a test armed pado_debug_fail_alloc for it -- and
+// counts itself live until released (pado_debug_live_allocations).
+void alloc_point();
+void alloc_live(int delta);
+
 // Owning device buffer.
 template <typename T>
 struct DBuf {
@@ -81,7 +88,11 @@ struct DBuf {
     void alloc(size_t count)
     {
         release();
-        if (count) PADO_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+        if (count) {
+            alloc_point();
+            PADO_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+            alloc_live(1);
+        }
         n = count;
     }
     // Stream-ordered allocation from the device's default memory pool (cheap
@@ -90,12 +101,19 @@ struct DBuf {
     void alloc_async(size_t count, cudaStream_t s)
     {
         release();
-        if (count) PADO_CUDA(cudaMallocAsync((void **)&p, count * sizeof(T), s));
+        if (count) {
+            alloc_point();
+            PADO_CUDA(cudaMallocAsync((void **)&p, count * sizeof(T), s));
+            alloc_live(1);
+        }
         n = count;
     }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p) {
+            cudaFree(p);
+            alloc_live(-1);
+        }
         p = nullptr;
         n = 0;
     }

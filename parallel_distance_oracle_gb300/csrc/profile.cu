@@ -106,9 +106,33 @@ void check_launch(const char *what)
     if (e != cudaSuccess) throw Error(PADO_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// ---- allocation accounting (failure-injection tests) ------------------------
+namespace {
+std::atomic<int64_t> g_fail_countdown{0};  // > 0: the allocation that brings it to 0 fails
+std::atomic<int64_t> g_live{0};            // device buffers of the library not yet released
+}  // namespace
+
+void alloc_point()
+{
+    if (g_fail_countdown.load(std::memory_order_relaxed) <= 0) return;
+    if (g_fail_countdown.fetch_sub(1) == 1)
+        throw Error(PADO_E_NOMEM, "device allocation failed (injected by pado_debug_fail_alloc)");
+}
+
+void alloc_live(int delta) { g_live.fetch_add(delta, std::memory_order_relaxed); }
+
 }  // namespace pado
 
 extern "C" {
+
+int pado_debug_fail_alloc(uint64_t nth)
+{
+    pado::g_fail_countdown.store((int64_t)nth);
+    return PADO_OK;
+}
+
+int64_t pado_debug_live_allocations(void) { return pado::g_live.load(); }
+
 
 uint64_t pado_kernel_launches(void) { return pado::g_launches.load(); }
 
