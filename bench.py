@@ -203,10 +203,88 @@ def run_reference(args, wl):
     out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": statistics.mean(secs) * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u8" if wl["kind"] == "unw" else "int16",
-           "data": "synthetic", "config": {"workload": args.workload, "desc": wl["desc"]},
+           "data": "synthetic",
+           "config": {"workload": args.workload, "desc": wl["desc"], "n": g.n, "m_directed": g.m_directed,
+                      "bp_roots": wl["K"], "batch": wl["B"], "l2": "inputs larger than L2 (graph + label state)",
+                      "parallelism": "host threads"},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": info["kind"], "sample": sample},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def query_cpu_baseline(idx, wl, qa, qb, gpu_answers):
+    """The reference's query_distance (pado_unw_unv_unp.h:1312-1445; weighted
+    pado_weighted_unv_unp.h:1782-1900) over the same canonical labels -- the
+    GPU index's, which equal the reference's own (full-size digest tests) --
+    and the same pairs, on the host: a single-thread loop as pado.cpp:105-125
+    runs it (bounded to the first 2M pairs) and an OpenMP loop over all pairs
+    on every host thread.  Its answers must equal the GPU's."""
+    from oracle import orc
+    K = wl["K"] if wl["kind"] == "unw" else 50
+    if not orc.ref_available(K):
+        return None
+    lab = idx.export()
+    n = idx.info().n
+    threads = os.cpu_count() or 1
+    a, b = np.ascontiguousarray(qa, np.uint32), np.ascontiguousarray(qb, np.uint32)
+    lib = orc.ref(K)
+
+    def run(k, t):
+        if wl["kind"] == "unw":
+            out = np.zeros(k, np.uint8)
+            secs = lib.ref_unw_query(n, lab.off, lab.hub, lab.dist, np.ascontiguousarray(lab.bpd),
+                                     np.ascontiguousarray(lab.bps), k, a, b, out, t)
+        else:
+            out = np.zeros(k, np.int16)
+            secs = lib.ref_w_query(n, lab.off, lab.hub, lab.dist, k, a, b, out, t)
+        return secs, out
+
+    k1 = min(len(a), 2_000_000)
+    s1, o1 = run(k1, 1)
+    sa, oa = run(len(a), threads)
+    assert np.array_equal(oa, gpu_answers) and np.array_equal(o1, gpu_answers[:k1]), \
+        "the reference's query answers differ from the GPU's"
+    log(f"reference query_distance: 1 thread {k1 / s1:.3e} q/s, {threads} threads {len(a) / sa:.3e} q/s")
+    return {"value": len(a) / sa, "unit": "queries/s", "cores": threads, "kind": "reference",
+            "sample": f"all {len(a)} pairs, OpenMP loop over the reference's query_distance on the same labels",
+            "single_thread_per_s": k1 / s1, "single_thread_sample": f"first {k1} pairs, one thread"}
+
+
+def sub_records(args):
+    """Compact records of the other configurations, each run as its own
+    bench.py process: weighted R-MAT s18 (labels/s, e2e, roofline, CPU
+    baseline), the many-graph labeler (batched vs one graph at a time) and the
+    serving loop (queries/s at p99 < 1 ms, against one launch per request)."""
+    runs = {
+        "weighted": ["--workload", "wrmat18", "--steps", "3", "--warmup", "3", "--queries", "1000000"]
+        + (["--no-cpu-baseline"] if args.no_cpu_baseline else []),
+        "many": ["--workload", "many", "--steps", "2", "--warmup", "1", "--no-profile"],
+        "serve": ["--workload", "serve", "--serve-rates", "1e5,3e5,1e6", "--serve-pairs", "1e7"],
+    }
+    out = {}
+    for name, argv in runs.items():
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run([sys.executable, str(REPO / "bench.py")] + argv, capture_output=True, text=True,
+                               timeout=900)
+            line = [ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1]
+            d = json.loads(line)
+        except Exception as e:  # a sub-record must not cost the main line
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
+            continue
+        keep = {"weighted": ("metric", "value", "unit", "ms_per_step", "dtype", "config", "e2e", "roofline",
+                             "cpu_baseline", "queries", "clocks", "gpu_launches", "labels"),
+                "many": ("metric", "value", "unit", "ms_per_step", "config", "labels", "batched", "one_at_a_time",
+                         "speedup_device", "speedup_wall", "tune", "e2e", "clocks", "gpu_launches"),
+                "serve": ("metric", "value", "unit", "config", "best_rate", "unbatched_value",
+                          "peak_batched_queries_per_s", "sweep", "clocks", "gpu_launches")}[name]
+        rec = {k: d.get(k) for k in keep}
+        if name == "weighted" and isinstance(rec.get("queries"), dict):
+            rec["queries"] = {k: rec["queries"].get(k) for k in ("n", "per_s_device", "per_s_e2e", "cpu_baseline")}
+        rec["seconds"] = time.perf_counter() - t0
+        out[name] = rec
+        log(f"sub-record {name}: {rec.get('value')} {rec.get('unit')} ({rec['seconds']:.0f}s)")
+    return out
 
 
 def w_prefix(g, rk, wl):
@@ -247,6 +325,12 @@ def main():
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--ingest-scale", type=int, default=INGEST["scale"],
                     help="R-MAT scale of the ingest workload's samples (smaller for ncu captures)")
+    ap.add_argument("--serve-rates", default=None,
+                    help="comma-separated arrival rates (req/s) of the serving sweep (default: the full sweep)")
+    ap.add_argument("--serve-pairs", type=float, default=SERVE["pairs_per_rate"],
+                    help="query pairs replayed per arrival rate")
+    ap.add_argument("--no-subrecords", action="store_true",
+                    help="default workload only: skip the weighted / many-graph / serving sub-records")
     args = ap.parse_args()
     if args.workload == "many":
         return run_many(args)
@@ -441,6 +525,16 @@ def main():
         cpu = {"value": r["labels"] / r["seconds"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
                "sample": sample, "seconds": r["seconds"], "labels": r["labels"]}
 
+    # ---- CPU query baseline: the reference's query_distance, same labels and pairs ----
+    qcpu = None
+    if not args.no_cpu_baseline and grank == 0:
+        qcpu = query_cpu_baseline(idx, wl, qa, qb, host_out)
+
+    # ---- sub-records: the weighted, many-graph and serving configurations ----
+    subs = None
+    if world == 1 and args.workload == "rmat20" and not args.no_subrecords:
+        subs = sub_records(args)
+
     if grank == 0:
         out = {
             "metric": METRIC, "value": replica_throughput(labels, world, dev_mean), "unit": UNIT, "n_gpus": world,
@@ -453,7 +547,9 @@ def main():
             "labels": labels, "labeling_s": dev_mean, "bp_s": info.bp_seconds, "levels": info.levels,
             "e2e": {"value": replica_throughput(labels, world, wall_mean), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "wall_s": wall_mean},
-            "queries": {"n": nq, "per_s_device": nq / q_dev_s, "per_s_e2e": nq / q_e2e_s, "roofline": q_roof},
+            "queries": {"n": nq, "per_s_device": nq / q_dev_s, "per_s_e2e": nq / q_e2e_s, "roofline": q_roof,
+                        "cpu_baseline": qcpu},
+            "sub_records": subs,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
             "profile": prof,
         }
@@ -986,7 +1082,7 @@ def run_serve(args):
 
     def trace(rate):
         mean_k = (SERVE["kmax"] - 1) / np.log(SERVE["kmax"])
-        nreq = int(max(500, min(40_000, SERVE["pairs_per_rate"] / mean_k)))
+        nreq = int(max(500, min(40_000, args.serve_pairs / mean_k)))
         arrival = np.cumsum(rng.exponential(1.0 / rate, size=nreq))
         ids = rng.integers(0, len(sets), size=nreq).astype(np.uint32)
         ks = np.minimum(np.exp(rng.uniform(0, np.log(SERVE["kmax"] + 1), size=nreq)).astype(np.uint64),
@@ -1008,8 +1104,9 @@ def run_serve(args):
     sweep = []
     checks = []
     launches0 = lib.pado_kernel_launches()
+    rates = [float(x) for x in args.serve_rates.split(",")] if args.serve_rates else SERVE["rates"]
     with ClockSampler(0) as clk:
-        for rate in SERVE["rates"]:
+        for rate in rates:
             arrival, ids, ks, a, b = trace(rate)
             row = {"rate_req_s": rate, "requests": int(len(ks)), "pairs": int(ks.sum())}
             for mode, name in ((0, "batched"), (1, "unbatched")):
