@@ -503,7 +503,17 @@ def main():
         roofline = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                     "frac": (ach / peak) if ach else None, "traffic": traffic_from_profiles(top, args.workload),
                     "peak_source": peak_src, "share_of_labeling_device_time": tk["ms"] / tot_ms if tot_ms else None,
-                    "launches": tk["launches"], "avg_launch_us": avg_s * 1e6, "bytes_per_launch": per_launch_bytes}
+                    "launches": tk["launches"], "avg_launch_us": avg_s * 1e6, "bytes_per_launch": per_launch_bytes,
+                    "bytes_source": "device-counted bytes of this implementation"}
+        fb = formula_bytes(top, prof, args.workload, wl)
+        if fb:
+            # the per-event formula over the reference algorithm's events is
+            # the algorithmic figure; the implementation's own count is kept
+            # beside it (it skips most of the formula's BP-row bytes)
+            roofline.update({"achieved": fb["bytes"] / avg_s / 1e9, "frac": fb["bytes"] / avg_s / 1e9 / peak,
+                             "bytes_per_launch": fb["bytes"], "bytes_terms": fb["terms"],
+                             "bytes_source": fb["source"], "device_counted_bytes_per_launch": per_launch_bytes,
+                             "achieved_device_counted": ach, "frac_device_counted": (ach / peak) if ach else None})
     qk = "query_unw_kernel" if wl["kind"] == "unw" else "query_w_kernel"
     q_roof = None
     if qk in prof and prof[qk]["bytes"]:
@@ -842,6 +852,53 @@ def run_ingest(args):
             "profile": prof}), flush=True)
     if pg:
         pg.destroy_process_group()
+
+
+def formula_terms(workload: str):
+    """Per-event byte terms of the reference algorithm for `workload`, from
+    the committed table profiles/algorithmic_bytes.md (written by
+    oracle/count_events.py): {term: bytes}."""
+    path = REPO / "profiles" / "algorithmic_bytes.md"
+    if not path.exists():
+        return None
+    out = {}
+    for ln in path.read_text().splitlines():
+        cells = [c.strip() for c in ln.strip().strip("|").split("|")]
+        if len(cells) >= 3 and cells[0] == workload:
+            try:
+                out[cells[1]] = int(cells[2])
+            except ValueError:
+                continue
+    return out or None
+
+
+def formula_bytes(kernel: str, prof: dict, workload: str, wl: dict):
+    """Algorithmic bytes of one launch of the labeling loop by the per-event
+    formula.  Unweighted: 17*K B per BP test and 5 B per label appended,
+    both counted by the device in this run (the same events as the
+    reference's order), plus the push-order terms the device does not count
+    (4 B per adjacency entry scanned by push, 5 B per distance-test entry,
+    8 B per queue entry) from the oracle's counts for the same workload.
+    Weighted: every term from the oracle's counts."""
+    terms = formula_terms(workload)
+    if not terms or prof.get(kernel, {}).get("launches", 0) != 1:
+        return None
+    if kernel == "label_loop_kernel" and wl["kind"] == "unw":
+        offers = prof.get("events.first_offers", {}).get("bytes", 0)
+        labels = prof.get("events.labels_appended", {}).get("bytes", 0)
+        if not offers or not labels:
+            return None
+        t = {"bp_tests": 17 * wl["K"] * offers, "labels_appended": 5 * labels,
+             "push_edges": terms.get("push_edges", 0), "distance_entries": terms.get("distance_entries", 0),
+             "queues": terms.get("queues", 0)}
+        src = ("per-event formula: BP tests and labels appended counted by the device in this run, push-order "
+               "terms from the oracle's event counts (profiles/algorithmic_bytes.md)")
+    elif kernel == "w_loop_kernel" and wl["kind"] == "w":
+        t = {k: terms[k] for k in ("edges", "check_entries", "labels_appended", "relaxations") if k in terms}
+        src = "per-event formula over the oracle's event counts (profiles/algorithmic_bytes.md)"
+    else:
+        return None
+    return {"bytes": sum(t.values()), "terms": t, "source": src}
 
 
 def attribute_loop_bytes(prof):

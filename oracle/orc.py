@@ -42,7 +42,7 @@ class WLabels:
 
 
 UNW_STATS = ["batches", "levels", "head_visits", "edges_scanned", "pairs_offered", "bp_checks",
-             "bp_pruned", "dist_checks", "dist_entries", "labels_added", "root_rows"]
+             "bp_pruned", "dist_checks", "dist_entries", "labels_added", "root_rows", "cand_vertices"]
 W_STATS = ["batches", "rounds", "edges_scanned", "relax_tries", "relax_accepted", "checks",
            "check_entries", "temp_labels", "filtered", "labels_added"]
 

@@ -191,6 +191,7 @@ struct UnwStats {
     uint64_t dist_entries = 0;     // label entries inspected by distance_query
     uint64_t labels_added = 0;     // labels inserted (root self labels included)
     uint64_t root_rows = 0;        // dist_matrix cells written at batch start
+    uint64_t cand_vertices = 0;    // candidate-queue entries (vertices given candidates in a level)
 };
 
 struct UnwLabeler {
@@ -359,7 +360,7 @@ struct UnwLabeler {
                     continue;
                 }
                 cand_roots[t].push_back(rr - s);
-                if (!got_cand[t]) { got_cand[t] = 1; cand_q.push_back(t); }
+                if (!got_cand[t]) { got_cand[t] = 1; cand_q.push_back(t); ++st.cand_vertices; }
             }
         }
     }
@@ -811,13 +812,14 @@ void orc_unw_export(const orc_unw *h, uint64_t *off, uint32_t *hub, uint8_t *dis
 }
 
 // stats: batches, levels, head_visits, edges_scanned, pairs_offered,
-// bp_checks, bp_pruned, dist_checks, dist_entries, labels_added, root_rows
+// bp_checks, bp_pruned, dist_checks, dist_entries, labels_added, root_rows,
+// cand_vertices
 void orc_unw_stats(const orc_unw *h, uint64_t *out)
 {
     const UnwStats &s = h->st;
     uint64_t v[] = {s.batches, s.levels, s.head_visits, s.edges_scanned, s.pairs_offered,
                     s.bp_checks, s.bp_pruned, s.dist_checks, s.dist_entries, s.labels_added,
-                    s.root_rows};
+                    s.root_rows, s.cand_vertices};
     memcpy(out, v, sizeof(v));
 }
 

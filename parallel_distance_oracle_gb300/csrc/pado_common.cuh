@@ -221,7 +221,11 @@ void prof_end(const char *name, cudaStream_t s);
 enum WorkSlot : int {
     W_PULL = 0, W_MARK, W_BP_SIB, W_BP_CHILD, W_Q_UNW, W_Q_W, W_WPULL, W_WMARK, W_FINAL,
     // pull_kernel phase cycles (light tails, summed over warps)
-    W_CYC_SCAN, W_CYC_BP, W_CYC_DIST, W_CYC_COMMIT, W_CYC_HEAVY, WORK_SLOTS
+    W_CYC_SCAN, W_CYC_BP, W_CYC_DIST, W_CYC_COMMIT, W_CYC_HEAVY,
+    // event counts of the unweighted labeling: first offers of a root to a
+    // tail in a batch (each one BP test) and labels appended (self labels
+    // included) -- the same events as the reference's push order counts
+    W_EV_OFFERS, W_EV_LABELS, WORK_SLOTS
 };
 const char *work_slot_name(int i);
 unsigned long long *work_counters();

@@ -70,7 +70,8 @@ const char *work_slot_name(int i)
                                             "bp_child_kernel",  "query_unw_kernel", "query_w_kernel",
                                             "w_pull_kernel",    "w_mark_kernel",    "finalize_kernel",
                                             "pull.cycles.scan", "pull.cycles.bp",   "pull.cycles.dist",
-                                            "pull.cycles.commit", "pull.cycles.heavy"};
+                                            "pull.cycles.commit", "pull.cycles.heavy", "events.first_offers",
+                                            "events.labels_appended"};
     return names[i];
 }
 

@@ -150,6 +150,7 @@ __device__ void root_step_phase(const UnwDev &d, const uint32_t *roots, uint32_t
         for (uint32_t w = lane; w < d.words; w += 32)
             d.ind[(uint64_t)r * d.words + w] = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
         if (lane == 0) {
+            if (d.work) atomicAdd(&d.work[W_EV_LABELS], 1ull);
             d.pool_hub[base + len] = r;
             d.pool_dist[base + len] = 0;
             d.lab_len[r] = len + 1;

@@ -164,6 +164,7 @@ __device__ void root_init_phase(const UnwDev &d, const uint32_t *roots, uint32_t
         for (uint32_t w = lane; w < d.words; w += 32)
             d.ind[(uint64_t)r * d.words + w] = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
         if (lane == 0) {
+            if (d.work) atomicAdd(&d.work[W_EV_LABELS], 1ull);
             d.pool_hub[base + len] = r;
             d.pool_dist[base + len] = 0;
             d.lab_len[r] = len + 1;
@@ -525,6 +526,7 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     __syncthreads();
     const uint32_t noff = hs.ctr[0];
     if (noff == 0) return;  // uniform: nothing changed
+    if (d.work && tid == 0) atomicAdd(&d.work[W_EV_OFFERS], (unsigned long long)noff);
     // (b) BP test: thread per candidate on BP root 0, then warps take the
     // survivors one at a time over the remaining roots.
     if (tid == 0) bytes += 17ull * d.K;
@@ -652,6 +654,7 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         }
         __syncthreads();
         if (tid == 0) {
+            if (d.work) atomicAdd(&d.work[W_EV_LABELS], (unsigned long long)nadd);
             if (hs.ctr[6]) {
                 d.lab_off[t] = nbase;
                 d.lab_cap[t] = hs.ctr[7];
@@ -760,6 +763,7 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     __syncwarp();
     tick(W_CYC_SCAN);
     if (noff == 0) return;
+    if (d.work && lane == 0) atomicAdd(&d.work[W_EV_OFFERS], (unsigned long long)noff);
     bytes += 17ull + 4ull * d.words + 4;  // tail root-0 BP entry; indicator write-back
     // (c) BP test in two stages: lane per candidate on BP root 0 (which settles
     // most pairs), then warp-cooperative over the remaining roots for the rest.
@@ -936,6 +940,7 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         }
         mn = warp_min_u32(mn);
         bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0);
+        if (d.work && lane == 0) atomicAdd(&d.work[W_EV_LABELS], (unsigned long long)nadd);
         if (lane == 0) {
             d.lab_len[t] = len + nadd;
             d.last[cp][t] = LastGroup{base + len, nadd, a.lid_cur};

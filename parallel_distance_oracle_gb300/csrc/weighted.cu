@@ -345,21 +345,48 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
                     }
                 }
             }
-            if (i < ntouch) {
-                if (r != INT_MAX) {
-                    if (r == INT_MIN && b == 0) {
-                        const int16_t *crow = d.snap + (uint64_t)c * B;
-                        const uint16_t *tq = d.vq + (uint64_t)t * B;
-                        const int16_t *trow = d.vd + (uint64_t)t * B;
-                        for (uint32_t k = 0; k < vql; ++k) {
-                            const uint32_t rr = tq[k];
-                            if (creal <= s + rr) continue;
-                            const int16_t sc = crow[rr];
-                            if (sc == I16_INF) continue;
-                            const int32_t val = (int16_t)(trow[rr] + sc);
-                            if (val <= m) { r = val; break; }
+            // check (2) (batch 0 only), warp-uniform over t's temporary labels
+            // in first-acceptance order: a chunk of 32 (root, distance) pairs
+            // is loaded once and broadcast by shuffles, each lane still
+            // looking gathers 4 snapshot entries at a time and takes the first
+            // covering label in that order, as the reference's loop does
+            if (b == 0) {
+                bool look2 = r == INT_MIN;
+                const int16_t *crow = d.snap + (uint64_t)c * B;
+                const uint16_t *tqp = d.vq + (uint64_t)t * B;
+                const int16_t *trow = d.vd + (uint64_t)t * B;
+                for (uint32_t k0 = 0; k0 < vql && __any_sync(FULL, look2); k0 += 32) {
+                    const uint32_t kn = min(32u, vql - k0);
+                    const uint32_t rl = lane < (int)kn ? (uint32_t)tqp[k0 + lane] : 0u;
+                    const int32_t tl = lane < (int)kn ? (int32_t)trow[rl] : 0;
+                    for (uint32_t k = 0; k < kn; k += 4) {
+                        uint32_t rk[4];
+                        int32_t tk[4], sk[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            rk[u] = __shfl_sync(FULL, rl, (int)(k + u) & 31);
+                            tk[u] = __shfl_sync(FULL, tl, (int)(k + u) & 31);
+                        }
+                        if (look2) {
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                sk[u] = (k + u < kn && s + rk[u] < creal) ? (int32_t)crow[rk[u]] : (int32_t)I16_INF;
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                if (look2 && sk[u] != I16_INF) {
+                                    const int32_t val = (int16_t)(tk[u] + sk[u]);
+                                    if (val <= m) {
+                                        r = val;
+                                        look2 = false;
+                                    }
+                                }
+                            }
                         }
                     }
+                }
+            }
+            if (i < ntouch) {
+                if (r != INT_MAX) {
                     if (r == INT_MIN) {
                         acc = true;
                         isnew = d.vd[(uint64_t)t * B + c] == I16_INF;
