@@ -318,6 +318,9 @@ def main():
     ap.add_argument("--many-graphs", type=int, default=MANY["graphs"])
     ap.add_argument("--many-nmax", type=int, default=MANY["n_hi"])
     ap.add_argument("--many-batch", type=int, default=0, help="skip tuning and use this batch size")
+    ap.add_argument("--many-wave-labels", type=float, default=0,
+                    help="label the graphs in consecutive waves of at most this many predicted labels, one "
+                         "pado_unw_build_many call each (0: all graphs in one call)")
     ap.add_argument("--queries", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-batches", type=int, default=None,
@@ -568,6 +571,15 @@ def main():
         pg.destroy_process_group()
 
 
+def predicted_labels(n: int, i: int) -> float:
+    """Label count of graph i of many_graphs() (even i: Erdos-Renyi, odd i:
+    grid) predicted from the counts measured on this workload's generators
+    at K = 50, B = 1024: ER 13.5M / 87.4M / 328.8M labels at n = 20k / 50k /
+    100k, grids 3.4M / 81.0M / 300.5M at n = 20k / 100k / 200k -- about
+    0.0926 n^1.91 and 0.0286 n^1.89.  Only used to size the waves."""
+    return 0.0926 * n ** 1.91 if i % 2 == 0 else 0.0286 * n ** 1.89
+
+
 def many_graphs(count, n_lo, n_hi, seed):
     rng = np.random.Generator(np.random.PCG64(seed))
     ns = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), size=count)).astype(np.int64)
@@ -610,13 +622,39 @@ def run_many(args):
                 "wall_s": time.perf_counter() - t}
         log(f"tuned batch size {B}: {tms}")
 
+    waves = [list(range(len(gs)))]
+    if args.many_wave_labels:
+        waves, cur, acc = [], [], 0.0
+        for i, g in enumerate(gs):
+            p = predicted_labels(g.n, i)
+            if cur and acc + p > args.many_wave_labels:
+                waves.append(cur)
+                cur, acc = [], 0.0
+            cur.append(i)
+            acc += p
+        waves.append(cur)
+        log(f"{len(waves)} waves of at most {args.many_wave_labels:.2e} predicted labels")
+
     def batched():
-        t0 = time.perf_counter()
-        idxs = pado.build_many(gs, ranks, bp_roots=K, batch=B)
-        wall = time.perf_counter() - t0
-        inf = idxs[0].info()
-        counts = [ix.info().num_labels for ix in idxs]
-        return idxs, inf.build_seconds, inf.bp_seconds, wall, counts, inf.levels
+        """All waves; the returned indexes are those of the last wave (the
+        earlier ones are closed as soon as they are counted)."""
+        dev = bp = wall = 0.0
+        counts, levels, idxs = [None] * len(gs), 0, []
+        for wv in waves:
+            t0 = time.perf_counter()
+            idxs = pado.build_many([gs[i] for i in wv], [ranks[i] for i in wv], bp_roots=K, batch=B)
+            wall += time.perf_counter() - t0
+            inf = idxs[0].info()
+            dev += inf.build_seconds
+            bp += inf.bp_seconds
+            levels += inf.levels
+            for i, ix in zip(wv, idxs):
+                counts[i] = ix.info().num_labels
+            if len(waves) > 1:
+                for ix in idxs:
+                    ix.close()
+                idxs = []
+        return idxs, dev, bp, wall, counts, levels
 
     for i in range(args.warmup):
         idxs, dev, bp, wall, counts, levels = batched()
@@ -654,7 +692,7 @@ def run_many(args):
     one_launches = lib.pado_kernel_launches() - l0
     assert one_counts == counts, "batched and one-at-a-time label counts differ"
     prof = {}
-    if not args.no_profile:
+    if not args.no_profile and len(waves) == 1:
         _lib.check(lib.pado_profile(1))
         for ix in pado.build_many(gs, ranks, bp_roots=K, batch=B):
             ix.close()
@@ -669,7 +707,8 @@ def run_many(args):
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": "many", "graphs": len(gs), "n_range": [MANY["n_lo"], args.many_nmax],
                    "n_total": n_tot, "mix": "half Erdos-Renyi avg degree 6, half grid + 2% long-range edges",
-                   "bp_roots": K, "batch": B, "l2": "inputs larger than L2 (graphs + label state)"},
+                   "bp_roots": K, "batch": B, "l2": "inputs larger than L2 (graphs + label state)",
+                   "waves": len(waves)},
         "labels": labels, "batched": {"device_s": dev_mean, "wall_s": wall_mean, "steps": levels,
                                       "gpu_launches_per_build": launches},
         "one_at_a_time": {"device_s": one_dev, "wall_s": one_wall, "gpu_launches": one_launches},
