@@ -18,8 +18,12 @@ PKG = Path(__file__).resolve().parent
 REPO = PKG.parent
 CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
-BUILD = PKG / "_build"
-LIB = PKG / "libpado_gpu.so"
+# PADO_DEBUG_BOUNDS=1 in the environment selects the bounds-checking build
+# (device index checks that record an error word instead of faulting; see
+# unw_device.cuh), kept beside the release library under its own name.
+DEBUG = os.environ.get("PADO_DEBUG_BOUNDS", "") not in ("", "0")
+BUILD = PKG / ("_build_debug" if DEBUG else "_build")
+LIB = PKG / ("libpado_gpu_debug.so" if DEBUG else "libpado_gpu.so")
 SOURCES = ["capi.cu", "query.cu", "bp.cu", "unw.cu", "unw_many.cu", "weighted.cu", "profile.cu", "noalloc.cu",
            "serve.cu", "ingest.cu", "selftest.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -50,6 +54,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     cc = nvcc()
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC),
                      "--expt-relaxed-constexpr"]
+    if DEBUG:
+        common += ["-DPADO_DEBUG_BOUNDS"]
     if verbose:
         common += ["-Xptxas", "-v"]
 

@@ -62,6 +62,20 @@ struct HostPhase {
     }
 };
 
+#ifdef PADO_DEBUG_BOUNDS
+// p[i] when i < lim; otherwise records `site` in *dbg and returns a reference
+// to a scratch slot (a write there is harmless, a read returns its bytes).
+__device__ __align__(16) static unsigned char g_dbg_sink[64];
+template <typename T>
+__device__ __forceinline__ T &dbg_ref(T *p, uint64_t i, uint64_t lim, uint32_t site, uint32_t *dbg)
+{
+    static_assert(sizeof(T) <= sizeof(g_dbg_sink), "scratch slot too small");
+    if (i < lim) return p[i];
+    if (dbg) atomicOr(dbg, 1u << site);
+    return *reinterpret_cast<T *>(g_dbg_sink);
+}
+#endif
+
 // Allocation accounting (profile.cu): every device buffer of the library
 // passes alloc_point() before it allocates -- which fails the allocation
 // with PADO_E_NOMEM when a test armed pado_debug_fail_alloc for it -- and

@@ -138,30 +138,31 @@ __device__ void root_step_phase(const UnwDev &d, const uint32_t *roots, uint32_t
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nr; q += nw) {
         const uint32_t r = roots[q];
         uint64_t base;
-        if (!warp_reserve(d, r, d.lab_len[r] + 1, base, lane)) {
+        if (!warp_reserve(d, r, UD_AT(d.lab_len, r, d.n, 1) + 1, base, lane)) {
             if (lane == 0) {
                 atomicOr(d.status, ST_POOL_RETRY);
                 bf.retry[atomicAdd(&c->retry_cnt, 1u)] = r;
             }
             continue;
         }
-        const uint32_t len = d.lab_len[r];
+        const uint32_t len = UD_AT(d.lab_len, r, d.n, 1);
         const uint32_t idx = r - s;
         for (uint32_t w = lane; w < d.words; w += 32)
-            d.ind[(uint64_t)r * d.words + w] = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
+            UD_AT(d.ind, (uint64_t)r * d.words + w, (uint64_t)d.n * d.words, 5) = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
         if (lane == 0) {
             if (d.work) atomicAdd(&d.work[W_EV_LABELS], 1ull);
-            d.pool_hub[base + len] = r;
-            d.pool_dist[base + len] = 0;
-            d.lab_len[r] = len + 1;
-            d.last[p][r] = LastGroup{base + len, 1u, L};
-            d.last_min[p][r] = r;
-            d.ind_stamp[r] = b + 1;
+            UD_AT(d.pool_hub, base + len, d.pool_cap, 2) = r;
+            UD_AT(d.pool_dist, base + len, d.pool_cap, 2) = 0;
+            UD_AT(d.lab_len, r, d.n, 1) = len + 1;
+            UD_AT(d.last[p], r, d.n, 1) = LastGroup{base + len, 1u, L};
+            UD_AT(d.last_min[p], r, d.n, 1) = r;
+            UD_AT(d.ind_stamp, r, d.n, 1) = b + 1;
         }
         __syncwarp();
         // dist_matrix row of r from all its labels, the new (r, 0) included
         uint8_t *row = dm + (uint64_t)idx * d.n;
-        for (uint32_t j = lane; j <= len; j += 32) row[d.pool_hub[base + j]] = d.pool_dist[base + j];
+        for (uint32_t j = lane; j <= len; j += 32)
+            UD_AT(row, UD_AT(d.pool_hub, base + j, d.pool_cap, 2), d.n, 4) = UD_AT(d.pool_dist, base + j, d.pool_cap, 2);
         mark_tails(d, r, r, L + 1, bf.tails[nx], &c->tcnt[nx], bf.htails[nx], &c->hcnt[nx], lane, 0, 1, bytes);
     }
     if (d.work && lane == 0 && bytes) atomicAdd(&d.work[W_MARK], bytes);
@@ -337,6 +338,12 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
     d.K = K;
     d.B = B;
     d.words = words;
+    d.m = g.m;
+#ifdef PADO_DEBUG_BOUNDS
+    DBuf<uint32_t> dbg_word(1);
+    dbg_word.fill_bytes(0, s);
+    d.dbg = dbg_word.p;
+#endif
     d.off = g.off.p;
     d.adj = g.adj.p;
     d.used = d_used.p;
@@ -638,6 +645,18 @@ LabelRun unw_label(const DevGraph &g, uint32_t K, uint32_t B, const std::vector<
             PADO_LAUNCH("finalize_kernel", s,
                         finalize_kernel<<<grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(d, out.off.p, out.hub.p, out.dist8.p));
         }
+#ifdef PADO_DEBUG_BOUNDS
+        {
+            uint32_t w = 0;
+            dbg_word.download(&w, 1, s);
+            PADO_CUDA(cudaStreamSynchronize(s));
+            if (w) {
+                char msg[96];
+                snprintf(msg, sizeof(msg), "device bounds check failed (sites mask 0x%x)", w);
+                throw Error(PADO_E_STATE, msg);
+            }
+        }
+#endif
         PADO_CUDA(cudaEventRecord(e1, s));
         PADO_CUDA(cudaEventSynchronize(e1));
         PADO_CUDA(cudaEventElapsedTime(&run.ms, e0, e1));

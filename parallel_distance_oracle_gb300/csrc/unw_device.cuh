@@ -28,8 +28,23 @@ struct __align__(16) LastGroup {
     uint32_t stamp;
 };
 
+// Device bounds checks of a PADO_DEBUG_BOUNDS build.  UD_AT(arr, i, lim, site)
+// is arr[i]; in such a build an index i >= lim sets bit `site` of the device
+// word d.dbg and the access goes to a scratch slot instead (never a trap), so
+// a run reports where it would have left its buffer and keeps going.  Sites:
+// 0 CSR, 1 per-vertex state, 2 label pool, 3 BP rows, 4 dist_matrix,
+// 5 indicator rows, 6 tail / frontier / retry lists.  Release builds compile
+// the checks away.
+#ifdef PADO_DEBUG_BOUNDS
+#define UD_AT(arr, i, lim, site) (::pado::dbg_ref((arr), (uint64_t)(i), (uint64_t)(lim), (site), d.dbg))
+#else
+#define UD_AT(arr, i, lim, site) ((arr)[i])
+#endif
+
 struct UnwDev {
     uint32_t n, K, B, words;
+    uint64_t m;             // adjacency entries
+    uint32_t *dbg;          // bounds-check error word (PADO_DEBUG_BOUNDS builds)
     const uint32_t *off;
     const uint32_t *adj;
     const uint8_t *used;    // per vertex: bit 0 BP vertex (never a tail), bit 1 heavy (degree >= HEAVY_DEG)
@@ -111,8 +126,8 @@ __device__ __forceinline__ uint32_t warp_min_u32(uint32_t v)
 // except pool_top, when the pool is exhausted.
 __device__ __forceinline__ bool warp_reserve(const UnwDev &d, uint32_t v, uint32_t need, uint64_t &base, int lane)
 {
-    const uint32_t len = d.lab_len[v], cap = d.lab_cap[v];
-    base = d.lab_off[v];
+    const uint32_t len = UD_AT(d.lab_len, v, d.n, 1), cap = UD_AT(d.lab_cap, v, d.n, 1);
+    base = UD_AT(d.lab_off, v, d.n, 1);
     if (need <= cap) return true;
     uint32_t ncap = max(max(2u * cap, need), 8u);
     ncap = (ncap + 7u) & ~7u;
@@ -121,13 +136,13 @@ __device__ __forceinline__ bool warp_reserve(const UnwDev &d, uint32_t v, uint32
     pos = __shfl_sync(FULL, pos, 0);
     if (pos + ncap > d.pool_cap) return false;
     for (uint32_t j = lane; j < len; j += 32) {
-        d.pool_hub[pos + j] = d.pool_hub[base + j];
-        d.pool_dist[pos + j] = d.pool_dist[base + j];
+        UD_AT(d.pool_hub, pos + j, d.pool_cap, 2) = UD_AT(d.pool_hub, base + j, d.pool_cap, 2);
+        UD_AT(d.pool_dist, pos + j, d.pool_cap, 2) = UD_AT(d.pool_dist, base + j, d.pool_cap, 2);
     }
     __syncwarp();
     if (lane == 0) {
-        d.lab_off[v] = pos;
-        d.lab_cap[v] = ncap;
+        UD_AT(d.lab_off, v, d.n, 1) = pos;
+        UD_AT(d.lab_cap, v, d.n, 1) = ncap;
     }
     base = pos;
     return true;
@@ -146,14 +161,14 @@ __device__ void root_init_phase(const UnwDev &d, const uint32_t *roots, uint32_t
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nroots; q += nw) {
         const uint32_t r = roots[q];
         uint64_t base;
-        if (!warp_reserve(d, r, d.lab_len[r] + 1, base, lane)) {
+        if (!warp_reserve(d, r, UD_AT(d.lab_len, r, d.n, 1) + 1, base, lane)) {
             if (lane == 0) {
                 atomicOr(d.status, ST_POOL_RETRY);
-                retry[atomicAdd(retry_cnt, 1u)] = r;
+                UD_AT(retry, atomicAdd(retry_cnt, 1u), d.n, 6) = r;
             }
             continue;
         }
-        const uint32_t len = d.lab_len[r];
+        const uint32_t len = UD_AT(d.lab_len, r, d.n, 1);
         uint32_t rs = s, rb = b;
         if (gmap) {
             const GDesc &x = gd[gmap[r]];
@@ -162,16 +177,16 @@ __device__ void root_init_phase(const UnwDev &d, const uint32_t *roots, uint32_t
         }
         const uint32_t idx = r - rs;
         for (uint32_t w = lane; w < d.words; w += 32)
-            d.ind[(uint64_t)r * d.words + w] = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
+            UD_AT(d.ind, (uint64_t)r * d.words + w, (uint64_t)d.n * d.words, 5) = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
         if (lane == 0) {
             if (d.work) atomicAdd(&d.work[W_EV_LABELS], 1ull);
-            d.pool_hub[base + len] = r;
-            d.pool_dist[base + len] = 0;
-            d.lab_len[r] = len + 1;
-            d.last[p][r] = LastGroup{base + len, 1u, lid0};
-            d.last_min[p][r] = r;
-            d.ind_stamp[r] = rb + 1;
-            front[atomicAdd(front_cnt, 1u)] = r;
+            UD_AT(d.pool_hub, base + len, d.pool_cap, 2) = r;
+            UD_AT(d.pool_dist, base + len, d.pool_cap, 2) = 0;
+            UD_AT(d.lab_len, r, d.n, 1) = len + 1;
+            UD_AT(d.last[p], r, d.n, 1) = LastGroup{base + len, 1u, lid0};
+            UD_AT(d.last_min[p], r, d.n, 1) = r;
+            UD_AT(d.ind_stamp, r, d.n, 1) = rb + 1;
+            UD_AT(front, atomicAdd(front_cnt, 1u), d.n, 6) = r;
         }
     }
 }
@@ -188,18 +203,20 @@ __device__ void dm_rows_phase(const UnwDev &d, const uint32_t *roots, uint32_t n
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nroots; q += nw) {
         const uint32_t r = roots[q];
         uint8_t *row;
-        uint32_t hb = 0;
+        uint32_t hb = 0, rn = d.n;
         if (gmap) {  // reset of a finished batch: its buffer is zqp
             const GDesc &x = gd[gmap[r]];
             hb = x.base;
+            rn = x.n;
             row = d.dm + x.dm_off + ((uint64_t)gd_u32(x.zqp) * d.B + (r - hb) % d.B) * x.n;
         } else {
             row = (dm ? dm : d.dm) + (uint64_t)(r - s) * d.n;
         }
-        const uint64_t base = d.lab_off[r];
-        const uint32_t len = d.lab_len[r];
+        const uint64_t base = UD_AT(d.lab_off, r, d.n, 1);
+        const uint32_t len = UD_AT(d.lab_len, r, d.n, 1);
         for (uint32_t j = lane; j < len; j += 32)
-            row[d.pool_hub[base + j] - hb] = fill ? d.pool_dist[base + j] : U8_INF;
+            UD_AT(row, UD_AT(d.pool_hub, base + j, d.pool_cap, 2) - hb, rn, 4) =
+                fill ? UD_AT(d.pool_dist, base + j, d.pool_cap, 2) : U8_INF;
     }
 }
 
@@ -214,25 +231,25 @@ __device__ void mark_phase(const UnwDev &d, const uint32_t *front, uint32_t cnt,
     unsigned long long bytes = 0;
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw) {
         const uint32_t h = front[q];
-        const uint32_t mn = d.last_min[pp][h];
-        const uint32_t e_end = d.off[h + 1];
+        const uint32_t mn = UD_AT(d.last_min[pp], h, d.n, 1);
+        const uint32_t e_end = UD_AT(d.off, h + 1, (uint64_t)d.n + 1, 0);
         bytes += 16;  // front entry, last_min, offsets
-        for (uint32_t e0 = d.off[h]; e0 < e_end; e0 += 32) {
+        for (uint32_t e0 = UD_AT(d.off, h, (uint64_t)d.n + 1, 0); e0 < e_end; e0 += 32) {
             const uint32_t e = e0 + lane;
             const bool in = e < e_end;
-            const uint32_t t = in ? d.adj[e] : 0u;
+            const uint32_t t = in ? UD_AT(d.adj, e, d.m, 0) : 0u;
             const bool ok = in && t > mn;
             if (d.work) bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
             bool appended = false;
-            const uint32_t f = ok ? d.used[t] : 1u;
-            const uint32_t ts = ok ? d.tail_stamp[t] : lid_cur;
+            const uint32_t f = ok ? UD_AT(d.used, t, d.n, 1) : 1u;
+            const uint32_t ts = ok ? UD_AT(d.tail_stamp, t, d.n, 1) : lid_cur;
             if (!(f & 1u) && ts != lid_cur) {
-                if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) {
+                if (atomicExch(&UD_AT(d.tail_stamp, t, d.n, 1), lid_cur) != lid_cur) {
                     const bool heavy = f & 2u;
                     if (heavy)
-                        htails[agg_append_by(htails_cnt, 1u)] = t;
+                        UD_AT(htails, agg_append_by(htails_cnt, 1u), d.n, 6) = t;
                     else
-                        tails[agg_append_by(tails_cnt, 0u)] = t;
+                        UD_AT(tails, agg_append_by(tails_cnt, 0u), d.n, 6) = t;
                     appended = true;
                 }
             }
@@ -448,23 +465,23 @@ __device__ __forceinline__ void mark_tails(const UnwDev &d, uint32_t h, uint32_t
                                            uint32_t w, uint32_t nw, unsigned long long &bytes,
                                            uint32_t *gcnt = nullptr)
 {
-    const uint32_t e_end = d.off[h + 1];
-    for (uint32_t e0 = d.off[h] + 32 * w; e0 < e_end; e0 += 32 * nw) {
+    const uint32_t e_end = UD_AT(d.off, h + 1, (uint64_t)d.n + 1, 0);
+    for (uint32_t e0 = UD_AT(d.off, h, (uint64_t)d.n + 1, 0) + 32 * w; e0 < e_end; e0 += 32 * nw) {
         const uint32_t e = e0 + lane;
         const bool in = e < e_end;
-        const uint32_t t = in ? d.adj[e] : 0u;
+        const uint32_t t = in ? UD_AT(d.adj, e, d.m, 0) : 0u;
         const bool ok = in && t > mn;
         if (d.work) bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ok)) * 5ull;
         bool appended = false;
         // flags and stamp are independent loads: one round trip
-        const uint32_t f = ok ? d.used[t] : 1u;
-        const uint32_t ts = ok ? d.tail_stamp[t] : stamp;
+        const uint32_t f = ok ? UD_AT(d.used, t, d.n, 1) : 1u;
+        const uint32_t ts = ok ? UD_AT(d.tail_stamp, t, d.n, 1) : stamp;
         if (!(f & 1u) && ts != stamp) {
-            if (atomicExch(&d.tail_stamp[t], stamp) != stamp) {
+            if (atomicExch(&UD_AT(d.tail_stamp, t, d.n, 1), stamp) != stamp) {
                 if (f & 2u)
-                    htails[agg_append_by(htails_cnt, 1u)] = t;
+                    UD_AT(htails, agg_append_by(htails_cnt, 1u), d.n, 6) = t;
                 else
-                    tails[agg_append_by(tails_cnt, 0u)] = t;
+                    UD_AT(tails, agg_append_by(tails_cnt, 0u), d.n, 6) = t;
                 appended = true;
             }
         }
@@ -486,19 +503,19 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     const uint32_t s = bc.s, iter = bc.iter;
     const int pp = (a.lid_cur - 1) & 1, cp = a.lid_cur & 1;
     const uint32_t lid_prev = a.lid_cur - 1;
-    const bool valid = d.ind_stamp[t] == bc.b + 1;
-    for (uint32_t x = tid; x < d.words; x += blockDim.x) hs.ind[x] = valid ? d.ind[(uint64_t)t * d.words + x] : 0u;
+    const bool valid = UD_AT(d.ind_stamp, t, d.n, 1) == bc.b + 1;
+    for (uint32_t x = tid; x < d.words; x += blockDim.x) hs.ind[x] = valid ? UD_AT(d.ind, (uint64_t)t * d.words + x, (uint64_t)d.n * d.words, 5) : 0u;
     if (tid < 9) hs.ctr[tid] = (tid == 4) ? 0xffffffffu : 0u;
     if (tid == 0) bytes += 8 + 8ull * d.words;
     __syncthreads();
     // (a) first offers from active neighbours, warps striding over the list
-    const uint32_t e_end = d.off[t + 1];
-    for (uint32_t e0 = d.off[t] + 32 * warp; e0 < e_end; e0 += 32 * (blockDim.x >> 5)) {
+    const uint32_t e_end = UD_AT(d.off, t + 1, (uint64_t)d.n + 1, 0);
+    for (uint32_t e0 = UD_AT(d.off, t, (uint64_t)d.n + 1, 0) + 32 * warp; e0 < e_end; e0 += 32 * (blockDim.x >> 5)) {
         const uint32_t e = e0 + lane;
         const bool in = e < e_end;
-        const uint32_t h = in ? d.adj[e] : 0u;
+        const uint32_t h = in ? UD_AT(d.adj, e, d.m, 0) : 0u;
         const bool ge = in && h >= s;
-        const LastGroup lg = ge ? d.last[pp][h] : LastGroup{0ull, 0u, 0u};
+        const LastGroup lg = ge ? UD_AT(d.last[pp], h, d.n, 1) : LastGroup{0ull, 0u, 0u};
         const bool act = ge && lg.stamp == lid_prev;
         uint32_t mask = __ballot_sync(FULL, act);
         if (lane == 0) bytes += __popc(__ballot_sync(FULL, in)) * 4ull + __popc(__ballot_sync(FULL, ge)) * 4ull;
@@ -512,7 +529,7 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             const uint32_t c = __shfl_sync(FULL, mcnt, src);
             if (lane == 0) bytes += 12 + 4ull * c;
             for (uint32_t j = lane; j < c; j += 32) {
-                const uint32_t r = d.pool_hub[pos + j];
+                const uint32_t r = UD_AT(d.pool_hub, pos + j, d.pool_cap, 2);
                 if (r < t) {
                     const uint32_t idx = r - s;
                     const uint32_t bit = 1u << (idx & 31);
@@ -531,20 +548,20 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     // survivors one at a time over the remaining roots.
     if (tid == 0) bytes += 17ull * d.K;
     const ulonglong2 zero2 = make_ulonglong2(0, 0);
-    const uint8_t td0 = lane < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane] : (uint8_t)U8_INF;
-    const uint8_t td1 = lane + 32 < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane + 32] : (uint8_t)U8_INF;
-    const ulonglong2 ts0 = lane < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane] : zero2;
+    const uint8_t td0 = lane < (int)d.K ? UD_AT(d.bpd, (uint64_t)t * d.K + lane, (uint64_t)d.n * d.K, 3) : (uint8_t)U8_INF;
+    const uint8_t td1 = lane + 32 < (int)d.K ? UD_AT(d.bpd, (uint64_t)t * d.K + lane + 32, (uint64_t)d.n * d.K, 3) : (uint8_t)U8_INF;
+    const ulonglong2 ts0 = lane < (int)d.K ? UD_AT(reinterpret_cast<const ulonglong2 *>(d.bps), (uint64_t)t * d.K + lane, (uint64_t)d.n * d.K, 3) : zero2;
     const ulonglong2 ts1 =
-        lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
+        lane + 32 < (int)d.K ? UD_AT(reinterpret_cast<const ulonglong2 *>(d.bps), (uint64_t)t * d.K + lane + 32, (uint64_t)d.n * d.K, 3) : zero2;
     const uint8_t tr0d = __shfl_sync(FULL, td0, 0);
     const ulonglong2 tr0s = make_ulonglong2(__shfl_sync(FULL, ts0.x, 0), __shfl_sync(FULL, ts0.y, 0));
-    const uint32_t tmin = d.K ? d.bpmin[t] : (uint32_t)U8_INF;
+    const uint32_t tmin = d.K ? UD_AT(d.bpmin, t, d.n, 1) : (uint32_t)U8_INF;
     for (uint32_t c = tid; c < noff; c += blockDim.x) {
         const uint16_t idx = hs.offered[c];
         const uint64_t rr = s + idx;
-        if (d.K == 0 || (uint32_t)d.bpmin[rr] + tmin > iter + 2u)  // cannot be covered: no second stage
+        if (d.K == 0 || (uint32_t)UD_AT(d.bpmin, rr, d.n, 1) + tmin > iter + 2u)  // cannot be covered: no second stage
             hs.surv[atomicAdd(&hs.ctr[1], 1u)] = idx | 0x8000u;
-        else if (!bp_one(d.bpd[rr * d.K], reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K], tr0d, tr0s, iter))
+        else if (!bp_one(UD_AT(d.bpd, rr * d.K, (uint64_t)d.n * d.K, 3), UD_AT(reinterpret_cast<const ulonglong2 *>(d.bps), rr * d.K, (uint64_t)d.n * d.K, 3), tr0d, tr0s, iter))
             hs.surv[atomicAdd(&hs.ctr[1], 1u)] = idx;
     }
     __syncthreads();
@@ -569,16 +586,16 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         for (uint32_t c = tid; c < nsurv1; c += blockDim.x) hs.surv[c] &= 0x7fffu;
         __syncthreads();
     }
-    const uint32_t len = d.lab_len[t];
-    const uint64_t base = d.lab_off[t];
+    const uint32_t len = UD_AT(d.lab_len, t, d.n, 1);
+    const uint64_t base = UD_AT(d.lab_off, t, d.n, 1);
     // (c) distance test
     if (nsurv) {
         for (uint32_t j = tid; j < len; j += blockDim.x) {
-            const uint8_t dd = d.pool_dist[base + j];
+            const uint8_t dd = UD_AT(d.pool_dist, base + j, d.pool_cap, 2);
             if (dd < iter) {
                 const uint32_t slot = atomicAdd(&hs.ctr[2], 1u);
                 if (slot < HSMALL_CAP) {
-                    hs.sh[slot] = d.pool_hub[base + j];
+                    hs.sh[slot] = UD_AT(d.pool_hub, base + j, d.pool_cap, 2);
                     hs.sd[slot] = dd;
                 }
             }
@@ -594,14 +611,14 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             if (nsmall <= HSMALL_CAP) {
                 for (uint32_t k = 0; k < nsmall; ++k) {
                     const uint32_t hh = hs.sh[k];
-                    if (hh < rr && (uint32_t)hs.sd[k] + (uint32_t)row[hh - bc.base] <= iter) { keep = false; break; }
+                    if (hh < rr && (uint32_t)hs.sd[k] + (uint32_t)UD_AT(row, hh - bc.base, bc.dn, 4) <= iter) { keep = false; break; }
                 }
             } else {
                 for (uint32_t j = 0; j < len; ++j) {
-                    const uint32_t dd = d.pool_dist[base + j];
+                    const uint32_t dd = UD_AT(d.pool_dist, base + j, d.pool_cap, 2);
                     if (dd >= iter) continue;
-                    const uint32_t hh = d.pool_hub[base + j];
-                    if (hh < rr && dd + (uint32_t)row[hh - bc.base] <= iter) { keep = false; break; }
+                    const uint32_t hh = UD_AT(d.pool_hub, base + j, d.pool_cap, 2);
+                    if (hh < rr && dd + (uint32_t)UD_AT(row, hh - bc.base, bc.dn, 4) <= iter) { keep = false; break; }
                 }
             }
             if (keep) hs.offered[atomicAdd(&hs.ctr[3], 1u)] = idx;
@@ -612,7 +629,7 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     if (nadd) {
         // (d) reserve, relocating if the slot is too small
         if (tid == 0) {
-            const uint32_t cap = d.lab_cap[t], need = len + nadd;
+            const uint32_t cap = UD_AT(d.lab_cap, t, d.n, 1), need = len + nadd;
             hs.ctr[5] = 1;
             hs.ctr[6] = 0;
             *hs.base = base;
@@ -633,36 +650,36 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         if (!hs.ctr[5]) {
             if (tid == 0) {
                 atomicOr(d.status, ST_POOL_RETRY);
-                a.retry[atomicAdd(a.retry_cnt, 1u)] = t;
+                UD_AT(a.retry, atomicAdd(a.retry_cnt, 1u), d.n, 6) = t;
             }
             return;  // uniform; nothing committed
         }
         const uint64_t nbase = *hs.base;
         if (hs.ctr[6]) {
             for (uint32_t j = tid; j < len; j += blockDim.x) {
-                d.pool_hub[nbase + j] = d.pool_hub[base + j];
-                d.pool_dist[nbase + j] = d.pool_dist[base + j];
+                UD_AT(d.pool_hub, nbase + j, d.pool_cap, 2) = UD_AT(d.pool_hub, base + j, d.pool_cap, 2);
+                UD_AT(d.pool_dist, nbase + j, d.pool_cap, 2) = UD_AT(d.pool_dist, base + j, d.pool_cap, 2);
             }
         }
         const bool is_root = t >= s && t < bc.e;
         for (uint32_t j = tid; j < nadd; j += blockDim.x) {
             const uint32_t idx = hs.offered[j];
-            d.pool_hub[nbase + len + j] = s + idx;
-            d.pool_dist[nbase + len + j] = (uint8_t)iter;
-            if (is_root) bc.dm[(uint64_t)(t - s) * bc.dn + (s + idx - bc.base)] = (uint8_t)iter;
+            UD_AT(d.pool_hub, nbase + len + j, d.pool_cap, 2) = s + idx;
+            UD_AT(d.pool_dist, nbase + len + j, d.pool_cap, 2) = (uint8_t)iter;
+            if (is_root) UD_AT(bc.dm, (uint64_t)(t - s) * bc.dn + (s + idx - bc.base), (uint64_t)d.B * bc.dn, 4) = (uint8_t)iter;
             atomicMin(&hs.ctr[4], s + idx);
         }
         __syncthreads();
         if (tid == 0) {
             if (d.work) atomicAdd(&d.work[W_EV_LABELS], (unsigned long long)nadd);
             if (hs.ctr[6]) {
-                d.lab_off[t] = nbase;
-                d.lab_cap[t] = hs.ctr[7];
+                UD_AT(d.lab_off, t, d.n, 1) = nbase;
+                UD_AT(d.lab_cap, t, d.n, 1) = hs.ctr[7];
             }
-            d.lab_len[t] = len + nadd;
-            d.last[cp][t] = LastGroup{nbase + len, nadd, a.lid_cur};
-            d.last_min[cp][t] = hs.ctr[4];
-            if (!a.next_tails) a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
+            UD_AT(d.lab_len, t, d.n, 1) = len + nadd;
+            UD_AT(d.last[cp], t, d.n, 1) = LastGroup{nbase + len, nadd, a.lid_cur};
+            UD_AT(d.last_min[cp], t, d.n, 1) = hs.ctr[4];
+            if (!a.next_tails) UD_AT(a.front_next, atomicAdd(a.front_next_cnt, 1u), d.n, 6) = t;
             bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0) + (hs.ctr[6] ? 10ull * len : 0);
         }
         if (a.next_tails)
@@ -670,8 +687,8 @@ __device__ void pull_heavy_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
                        a.next_htails_cnt, lane, warp, blockDim.x >> 5, bytes,
                        a.gd_mut ? &a.gd_mut[bc.g].tc[a.next_stamp % 3] : nullptr);
     }
-    for (uint32_t x = tid; x < d.words; x += blockDim.x) d.ind[(uint64_t)t * d.words + x] = hs.ind[x];
-    if (tid == 0) d.ind_stamp[t] = bc.b + 1;
+    for (uint32_t x = tid; x < d.words; x += blockDim.x) UD_AT(d.ind, (uint64_t)t * d.words + x, (uint64_t)d.n * d.words, 5) = hs.ind[x];
+    if (tid == 0) UD_AT(d.ind_stamp, t, d.n, 1) = bc.b + 1;
 }
 
 // One light tail, processed by one warp.
@@ -694,8 +711,8 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     const uint32_t lid_prev = a.lid_cur - 1;
     bytes += 8 + 4ull * d.words;  // tail entry, indicator stamp and row
     // (a) indicator row of t for this batch
-    const bool valid = d.ind_stamp[t] == bc.b + 1;
-    for (uint32_t x = lane; x < d.words; x += 32) wr.ind[x] = valid ? d.ind[(uint64_t)t * d.words + x] : 0u;
+    const bool valid = UD_AT(d.ind_stamp, t, d.n, 1) == bc.b + 1;
+    for (uint32_t x = lane; x < d.words; x += 32) wr.ind[x] = valid ? UD_AT(d.ind, (uint64_t)t * d.words + x, (uint64_t)d.n * d.words, 5) : 0u;
     uint32_t noff = 0;  // first offers so far, in wr.offered
     __syncwarp();
     // (b) gather first offers from active neighbours (heads >= s), 64
@@ -703,15 +720,15 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     // flattened into one item list (inclusive counts sa / sb over the two
     // halves) and spread over the lanes, so one round of loads covers 32 hubs
     // whichever heads they belong to.
-    const uint32_t e_end = d.off[t + 1];
-    for (uint32_t e0 = d.off[t]; e0 < e_end; e0 += 64) {
+    const uint32_t e_end = UD_AT(d.off, t + 1, (uint64_t)d.n + 1, 0);
+    for (uint32_t e0 = UD_AT(d.off, t, (uint64_t)d.n + 1, 0); e0 < e_end; e0 += 64) {
         const uint32_t ea = e0 + lane, eb = ea + 32;
         const bool ina = ea < e_end, inb = eb < e_end;
-        const uint32_t ha = ina ? d.adj[ea] : 0u, hb = inb ? d.adj[eb] : 0u;
+        const uint32_t ha = ina ? UD_AT(d.adj, ea, d.m, 0) : 0u, hb = inb ? UD_AT(d.adj, eb, d.m, 0) : 0u;
         const bool gea = ina && ha >= s, geb = inb && hb >= s;
         // every head's newest group (stamp, position, size): one load each, in parallel
-        const LastGroup la = gea ? d.last[pp][ha] : LastGroup{0ull, 0u, 0u};
-        const LastGroup lb = geb ? d.last[pp][hb] : LastGroup{0ull, 0u, 0u};
+        const LastGroup la = gea ? UD_AT(d.last[pp], ha, d.n, 1) : LastGroup{0ull, 0u, 0u};
+        const LastGroup lb = geb ? UD_AT(d.last[pp], hb, d.n, 1) : LastGroup{0ull, 0u, 0u};
         const bool acta = gea && la.stamp == lid_prev, actb = geb && lb.stamp == lid_prev;
         const uint64_t pa = acta ? la.pos : 0ull, pb = actb ? lb.pos : 0ull;
         const uint32_t ca = acta ? la.cnt : 0u, cb = actb ? lb.cnt : 0u;
@@ -745,7 +762,7 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             bool fresh = false;
             uint32_t idx = 0;
             if (i < tot) {
-                const uint32_t r = d.pool_hub[(second ? qb : qa) + (key - (second ? xb : xa))];
+                const uint32_t r = UD_AT(d.pool_hub, (second ? qb : qa) + (key - (second ? xb : xa)), d.pool_cap, 2);
                 if (r < t) {
                     idx = r - s;
                     const uint32_t bit = 1u << (idx & 31);
@@ -771,7 +788,7 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     // Any root i gives td_i >= bpmin[r] + bpmin[t], so a pair with
     // bpmin[r] + bpmin[t] - 2 > iter cannot be covered: it survives BP without
     // a row load (flag 0x8000: no second stage).
-    const uint32_t tmin = d.K ? d.bpmin[t] : (uint32_t)U8_INF;
+    const uint32_t tmin = d.K ? UD_AT(d.bpmin, t, d.n, 1) : (uint32_t)U8_INF;
     uint32_t nsurv = 0;
     bool need2 = false;  // some survivor needs the second stage
     for (uint32_t c0 = 0; c0 < noff; c0 += 32) {
@@ -783,11 +800,11 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             const uint64_t rr = s + idx;
             // the candidate's and the tail's root-0 entries (the latter the same
             // address in every lane) are independent loads: one round trip
-            const uint32_t bm = d.K ? d.bpmin[rr] : (uint32_t)U8_INF;
-            const uint8_t r0d = d.K ? d.bpd[rr * d.K] : (uint8_t)U8_INF;
-            const ulonglong2 r0s = d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[rr * d.K] : zero2;
-            const uint8_t t0d = d.K ? d.bpd[(uint64_t)t * d.K] : (uint8_t)U8_INF;
-            const ulonglong2 t0s = d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K] : zero2;
+            const uint32_t bm = d.K ? UD_AT(d.bpmin, rr, d.n, 1) : (uint32_t)U8_INF;
+            const uint8_t r0d = d.K ? UD_AT(d.bpd, rr * d.K, (uint64_t)d.n * d.K, 3) : (uint8_t)U8_INF;
+            const ulonglong2 r0s = d.K ? UD_AT(reinterpret_cast<const ulonglong2 *>(d.bps), rr * d.K, (uint64_t)d.n * d.K, 3) : zero2;
+            const uint8_t t0d = d.K ? UD_AT(d.bpd, (uint64_t)t * d.K, (uint64_t)d.n * d.K, 3) : (uint8_t)U8_INF;
+            const ulonglong2 t0s = d.K ? UD_AT(reinterpret_cast<const ulonglong2 *>(d.bps), (uint64_t)t * d.K, (uint64_t)d.n * d.K, 3) : zero2;
             if (d.K == 0 || bm + tmin > iter + 2u) {
                 keep = true;
                 ent = idx | 0x8000u;
@@ -806,12 +823,12 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     if (d.K > 1 && need2) {
         // second stage for the unflagged survivors, two candidates per step,
         // against t's whole row (lane i: roots i and i + 32), loaded only now
-        const uint8_t td0 = lane < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane] : (uint8_t)U8_INF;
-        const uint8_t td1 = lane + 32 < (int)d.K ? d.bpd[(uint64_t)t * d.K + lane + 32] : (uint8_t)U8_INF;
+        const uint8_t td0 = lane < (int)d.K ? UD_AT(d.bpd, (uint64_t)t * d.K + lane, (uint64_t)d.n * d.K, 3) : (uint8_t)U8_INF;
+        const uint8_t td1 = lane + 32 < (int)d.K ? UD_AT(d.bpd, (uint64_t)t * d.K + lane + 32, (uint64_t)d.n * d.K, 3) : (uint8_t)U8_INF;
         const ulonglong2 ts0 =
-            lane < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane] : zero2;
+            lane < (int)d.K ? UD_AT(reinterpret_cast<const ulonglong2 *>(d.bps), (uint64_t)t * d.K + lane, (uint64_t)d.n * d.K, 3) : zero2;
         const ulonglong2 ts1 =
-            lane + 32 < (int)d.K ? reinterpret_cast<const ulonglong2 *>(d.bps)[(uint64_t)t * d.K + lane + 32] : zero2;
+            lane + 32 < (int)d.K ? UD_AT(reinterpret_cast<const ulonglong2 *>(d.bps), (uint64_t)t * d.K + lane + 32, (uint64_t)d.n * d.K, 3) : zero2;
         bytes += 17ull * (d.K - 1);
         uint32_t n2 = 0;
         for (uint32_t c0 = 0; c0 < nsurv; c0 += 32) {
@@ -855,8 +872,8 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
     // (ballot compaction, in list order); when they all fit, one staging
     // serves every candidate group.
     uint32_t nadd = 0;
-    const uint32_t len = d.lab_len[t];
-    uint64_t base = d.lab_off[t];
+    const uint32_t len = UD_AT(d.lab_len, t, d.n, 1);
+    uint64_t base = UD_AT(d.lab_off, t, d.n, 1);
     if (nsurv) {
         uint32_t nst = 0;
         // stage labels with d < iter from list position `from`; returns where it stopped
@@ -865,12 +882,12 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             for (; j < len && cnt + 32 <= (uint32_t)SMALL_CAP; j += 32) {
                 const uint32_t jj = j + lane;
                 const bool in = jj < len;
-                const uint8_t dd = in ? d.pool_dist[base + jj] : (uint8_t)U8_INF;
+                const uint8_t dd = in ? UD_AT(d.pool_dist, base + jj, d.pool_cap, 2) : (uint8_t)U8_INF;
                 const bool sm = in && dd < iter;
                 const uint32_t m = __ballot_sync(FULL, sm);
                 if (sm) {
                     const uint32_t p = cnt + __popc(m & ((1u << lane) - 1u));
-                    wr.sh[p] = d.pool_hub[base + jj];
+                    wr.sh[p] = UD_AT(d.pool_hub, base + jj, d.pool_cap, 2);
                     wr.sd[p] = (uint8_t)(iter - dd);  // slack: covered iff d(r, h) <= slack
                 }
                 cnt += __popc(m);
@@ -896,7 +913,9 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
                     // four dist_matrix gathers in flight per lane
                     for (; k + 4 <= nst; k += 4) {
                         const uint32_t h0 = wr.sh[k], h1 = wr.sh[k + 1], h2 = wr.sh[k + 2], h3 = wr.sh[k + 3];
-                        const uint32_t v0 = row[h0], v1 = row[h1], v2 = row[h2], v3 = row[h3];
+                        const uint64_t rl = (uint64_t)bc.base + bc.dn;
+                        const uint32_t v0 = UD_AT(row, h0, rl, 4), v1 = UD_AT(row, h1, rl, 4), v2 = UD_AT(row, h2, rl, 4),
+                                       v3 = UD_AT(row, h3, rl, 4);
                         if ((h0 < rr && v0 <= wr.sd[k]) || (h1 < rr && v1 <= wr.sd[k + 1]) ||
                             (h2 < rr && v2 <= wr.sd[k + 2]) || (h3 < rr && v3 <= wr.sd[k + 3])) {
                             keep = false;
@@ -905,7 +924,7 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
                     }
                     for (; keep && k < nst; ++k) {
                         const uint32_t hh = wr.sh[k];
-                        if (hh < rr && (uint32_t)row[hh] <= wr.sd[k]) keep = false;
+                        if (hh < rr && (uint32_t)UD_AT(row, hh, (uint64_t)bc.base + bc.dn, 4) <= wr.sd[k]) keep = false;
                     }
                 }
                 if (d.work) bytes += (uint64_t)__popc(__ballot_sync(FULL, c < nsurv)) * nst;
@@ -925,7 +944,7 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         if (!warp_reserve(d, t, len + nadd, base, lane)) {
             if (lane == 0) {
                 atomicOr(d.status, ST_POOL_RETRY);
-                a.retry[atomicAdd(a.retry_cnt, 1u)] = t;
+                UD_AT(a.retry, atomicAdd(a.retry_cnt, 1u), d.n, 6) = t;
             }
             return;  // nothing committed; re-run after the pool grows
         }
@@ -933,26 +952,26 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
         uint32_t mn = 0xffffffffu;
         for (uint32_t j = lane; j < nadd; j += 32) {
             const uint32_t idx = wr.offered[j];
-            d.pool_hub[base + len + j] = s + idx;
-            d.pool_dist[base + len + j] = (uint8_t)iter;
-            if (is_root) bc.dm[(uint64_t)(t - s) * bc.dn + (s + idx - bc.base)] = (uint8_t)iter;
+            UD_AT(d.pool_hub, base + len + j, d.pool_cap, 2) = s + idx;
+            UD_AT(d.pool_dist, base + len + j, d.pool_cap, 2) = (uint8_t)iter;
+            if (is_root) UD_AT(bc.dm, (uint64_t)(t - s) * bc.dn + (s + idx - bc.base), (uint64_t)d.B * bc.dn, 4) = (uint8_t)iter;
             mn = min(mn, s + idx);
         }
         mn = warp_min_u32(mn);
         bytes += 5ull * nadd + 28 + (is_root ? (uint64_t)nadd : 0);
         if (d.work && lane == 0) atomicAdd(&d.work[W_EV_LABELS], (unsigned long long)nadd);
         if (lane == 0) {
-            d.lab_len[t] = len + nadd;
-            d.last[cp][t] = LastGroup{base + len, nadd, a.lid_cur};
-            d.last_min[cp][t] = mn;
-            if (!a.next_tails) a.front_next[atomicAdd(a.front_next_cnt, 1u)] = t;
+            UD_AT(d.lab_len, t, d.n, 1) = len + nadd;
+            UD_AT(d.last[cp], t, d.n, 1) = LastGroup{base + len, nadd, a.lid_cur};
+            UD_AT(d.last_min[cp], t, d.n, 1) = mn;
+            if (!a.next_tails) UD_AT(a.front_next, atomicAdd(a.front_next_cnt, 1u), d.n, 6) = t;
         }
         if (a.next_tails)
             mark_tails(d, t, mn, a.next_stamp, a.next_tails, a.next_tails_cnt, a.next_htails, a.next_htails_cnt, lane,
                        0, 1, bytes, a.gd_mut ? &a.gd_mut[bc.g].tc[a.next_stamp % 3] : nullptr);
     }
-    for (uint32_t x = lane; x < d.words; x += 32) d.ind[(uint64_t)t * d.words + x] = wr.ind[x];
-    if (lane == 0) d.ind_stamp[t] = bc.b + 1;
+    for (uint32_t x = lane; x < d.words; x += 32) UD_AT(d.ind, (uint64_t)t * d.words + x, (uint64_t)d.n * d.words, 5) = wr.ind[x];
+    if (lane == 0) UD_AT(d.ind_stamp, t, d.n, 1) = bc.b + 1;
     __syncwarp();
     tick(W_CYC_COMMIT);
 }
@@ -1032,17 +1051,17 @@ __device__ void finalize_phase(const UnwDev &d, const uint64_t *fin_off, uint32_
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < d.n; v += nw) {
-        const uint64_t base = d.lab_off[v], fo = fin_off[v];
-        const uint32_t len = d.lab_len[v];
+        const uint64_t base = UD_AT(d.lab_off, v, d.n, 1), fo = fin_off[v];
+        const uint32_t len = UD_AT(d.lab_len, v, d.n, 1);
         const uint32_t gb = gmap ? gbase[gmap[v]] : 0u;
         uint32_t rs = 0;
         while (rs < len) {
-            const uint32_t batch = (d.pool_hub[base + rs] - gb) / d.B;
+            const uint32_t batch = (UD_AT(d.pool_hub, base + rs, d.pool_cap, 2) - gb) / d.B;
             // run end: first entry of a later batch (monotone by batch)
             uint32_t re = rs;
             for (;;) {
                 const uint32_t j = re + lane;
-                const bool same = j < len && (d.pool_hub[base + j] - gb) / d.B == batch;
+                const bool same = j < len && (UD_AT(d.pool_hub, base + j, d.pool_cap, 2) - gb) / d.B == batch;
                 const uint32_t m = __ballot_sync(FULL, same);
                 if (m == FULL) { re += 32; continue; }
                 re += __ffs(~m) - 1;
@@ -1051,12 +1070,12 @@ __device__ void finalize_phase(const UnwDev &d, const uint64_t *fin_off, uint32_
             for (uint32_t c0 = rs; c0 < re; c0 += 32) {
                 const uint32_t j = c0 + lane;
                 const bool mine = j < re;
-                const uint32_t key = mine ? d.pool_hub[base + j] : 0xffffffffu;
-                const uint8_t dist = mine ? d.pool_dist[base + j] : 0;
+                const uint32_t key = mine ? UD_AT(d.pool_hub, base + j, d.pool_cap, 2) : 0xffffffffu;
+                const uint8_t dist = mine ? UD_AT(d.pool_dist, base + j, d.pool_cap, 2) : 0;
                 uint32_t rank = 0;
                 for (uint32_t o0 = rs; o0 < re; o0 += 32) {
                     const uint32_t oj = o0 + lane;
-                    const uint32_t other = oj < re ? d.pool_hub[base + oj] : 0xffffffffu;
+                    const uint32_t other = oj < re ? UD_AT(d.pool_hub, base + oj, d.pool_cap, 2) : 0xffffffffu;
                     for (int k = 0; k < 32; ++k) rank += (__shfl_sync(FULL, other, k) < key) ? 1u : 0u;
                 }
                 if (mine) {

@@ -83,29 +83,30 @@ __device__ void many_root_step(const UnwDev &d, const ManyBufs &bf, ManyCtl *c, 
         const uint32_t gs = gd_u32(x.s), gb = gd_u32(x.b), gbase = x.base, gn = x.n;
         uint8_t *dm = d.dm + x.dm_off + (uint64_t)gd_u32(x.dmp) * d.B * gn;
         uint64_t base;
-        if (!warp_reserve(d, r, d.lab_len[r] + 1, base, lane)) {
+        if (!warp_reserve(d, r, UD_AT(d.lab_len, r, d.n, 1) + 1, base, lane)) {
             if (lane == 0) {
                 atomicOr(d.status, ST_POOL_RETRY);
                 bf.rretry[atomicAdd(&c->rretry_cnt, 1u)] = r;
             }
             continue;
         }
-        const uint32_t len = d.lab_len[r];
+        const uint32_t len = UD_AT(d.lab_len, r, d.n, 1);
         const uint32_t idx = r - gs;
         for (uint32_t w = lane; w < d.words; w += 32)
-            d.ind[(uint64_t)r * d.words + w] = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
+            UD_AT(d.ind, (uint64_t)r * d.words + w, (uint64_t)d.n * d.words, 5) = (w == (idx >> 5)) ? (1u << (idx & 31)) : 0u;
         if (lane == 0) {
             if (d.work) atomicAdd(&d.work[W_EV_LABELS], 1ull);
-            d.pool_hub[base + len] = r;
-            d.pool_dist[base + len] = 0;
-            d.lab_len[r] = len + 1;
-            d.last[p][r] = LastGroup{base + len, 1u, L};
-            d.last_min[p][r] = r;
-            d.ind_stamp[r] = gb + 1;
+            UD_AT(d.pool_hub, base + len, d.pool_cap, 2) = r;
+            UD_AT(d.pool_dist, base + len, d.pool_cap, 2) = 0;
+            UD_AT(d.lab_len, r, d.n, 1) = len + 1;
+            UD_AT(d.last[p], r, d.n, 1) = LastGroup{base + len, 1u, L};
+            UD_AT(d.last_min[p], r, d.n, 1) = r;
+            UD_AT(d.ind_stamp, r, d.n, 1) = gb + 1;
         }
         __syncwarp();
         uint8_t *row = dm + (uint64_t)idx * gn;
-        for (uint32_t j = lane; j <= len; j += 32) row[d.pool_hub[base + j] - gbase] = d.pool_dist[base + j];
+        for (uint32_t j = lane; j <= len; j += 32)
+            UD_AT(row, UD_AT(d.pool_hub, base + j, d.pool_cap, 2) - gbase, gn, 4) = UD_AT(d.pool_dist, base + j, d.pool_cap, 2);
         mark_tails(d, r, r, L + 1, bf.tails[nx], &c->tcnt[nx], bf.htails[nx], &c->hcnt[nx], lane, 0, 1, bytes,
                    &bf.gd[g].tc[nx]);
     }
@@ -354,6 +355,12 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
     d.K = K;
     d.B = B;
     d.words = words;
+    d.m = g.m;
+#ifdef PADO_DEBUG_BOUNDS
+    DBuf<uint32_t> dbg_word(1);
+    dbg_word.fill_bytes(0, s);
+    d.dbg = dbg_word.p;
+#endif
     d.off = g.off.p;
     d.adj = g.adj.p;
     d.used = d_used.p;
@@ -467,6 +474,18 @@ LabelRun unw_label_many(const DevGraph &g, const std::vector<uint32_t> &gbase, u
                         many_finalize_kernel<<<grid_for((uint64_t)n * 32, 256), 256, 0, s>>>(
                             d, out.off.p, out.hub.p, out.dist8.p, d_gmap.p, d_gbase.p));
         }
+#ifdef PADO_DEBUG_BOUNDS
+        {
+            uint32_t w = 0;
+            dbg_word.download(&w, 1, s);
+            PADO_CUDA(cudaStreamSynchronize(s));
+            if (w) {
+                char msg[96];
+                snprintf(msg, sizeof(msg), "device bounds check failed (sites mask 0x%x)", w);
+                throw Error(PADO_E_STATE, msg);
+            }
+        }
+#endif
         PADO_CUDA(cudaEventRecord(e1, s));
         PADO_CUDA(cudaEventSynchronize(e1));
         PADO_CUDA(cudaEventElapsedTime(&run.ms, e0, e1));
