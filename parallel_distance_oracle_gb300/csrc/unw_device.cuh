@@ -1040,20 +1040,60 @@ __device__ void pull_phase(const UnwDev &d, const PullArgs &a, unsigned char *pu
     __syncthreads();
 }
 
+constexpr int FIN_WARPS = 8;  // finalize kernels run blocks of 256 threads
+
 // Final store: copy every list out of the pool, sorting each batch run by hub.
 // Runs are contiguous because batches append in order; the batch of hub h is
 // (h - base) / B, base = first id of the vertex's graph (0 for one graph, else
 // gbase[gmap[v]]), and hubs are stored graph-local (h - base).  Entries are
-// unique per vertex, so a rank-by-count sort is exact.
+// unique per vertex, so ranking by count (short runs) or by a bitmap of the
+// batch's B ids (long runs) is exact.
 __device__ void finalize_phase(const UnwDev &d, const uint64_t *fin_off, uint32_t *fin_hub, uint8_t *fin_dist,
                                const uint16_t *gmap, const uint32_t *gbase)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    // per warp: a bitmap of one batch's ids and its words' prefix counts
+    __shared__ uint32_t fin_bm[FIN_WARPS][MAX_BATCH / 32], fin_pre[FIN_WARPS][MAX_BATCH / 32];
+    uint32_t *bm = fin_bm[threadIdx.x >> 5], *pre = fin_pre[threadIdx.x >> 5];
     for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < d.n; v += nw) {
         const uint64_t base = UD_AT(d.lab_off, v, d.n, 1), fo = fin_off[v];
         const uint32_t len = UD_AT(d.lab_len, v, d.n, 1);
         const uint32_t gb = gmap ? gbase[gmap[v]] : 0u;
+        if (len <= 128) {
+            // a short list: batch ranges are disjoint and ascending, so sorting
+            // the whole list by hub sorts every run; all of it is loaded in one
+            // round (lane i: entries i, i + 32, i + 64, i + 96) and each entry
+            // is ranked by counting the smaller hubs
+            uint32_t key[4];
+            uint8_t dist[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t j = lane + 32u * q;
+                key[q] = j < len ? UD_AT(d.pool_hub, base + j, d.pool_cap, 2) : 0xffffffffu;
+                dist[q] = j < len ? UD_AT(d.pool_dist, base + j, d.pool_cap, 2) : (uint8_t)0;
+            }
+            uint32_t rank[4] = {0, 0, 0, 0};
+            const uint32_t nq = (len + 31) / 32;
+#pragma unroll
+            for (int q2 = 0; q2 < 4; ++q2) {
+                if ((uint32_t)q2 >= nq) break;
+                for (int k = 0; k < 32; ++k) {
+                    const uint32_t other = __shfl_sync(FULL, key[q2], k);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) rank[q] += other < key[q] ? 1u : 0u;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t j = lane + 32u * q;
+                if (j < len) {
+                    fin_hub[fo + rank[q]] = key[q] - gb;
+                    fin_dist[fo + rank[q]] = dist[q];
+                }
+            }
+            continue;
+        }
         uint32_t rs = 0;
         while (rs < len) {
             const uint32_t batch = (UD_AT(d.pool_hub, base + rs, d.pool_cap, 2) - gb) / d.B;
@@ -1067,21 +1107,61 @@ __device__ void finalize_phase(const UnwDev &d, const uint64_t *fin_off, uint32_
                 re += __ffs(~m) - 1;
                 break;
             }
-            for (uint32_t c0 = rs; c0 < re; c0 += 32) {
-                const uint32_t j = c0 + lane;
+            if (re - rs <= 32) {
+                // a short run: rank by counting within one chunk
+                const uint32_t j = rs + lane;
                 const bool mine = j < re;
                 const uint32_t key = mine ? UD_AT(d.pool_hub, base + j, d.pool_cap, 2) : 0xffffffffu;
                 const uint8_t dist = mine ? UD_AT(d.pool_dist, base + j, d.pool_cap, 2) : 0;
                 uint32_t rank = 0;
-                for (uint32_t o0 = rs; o0 < re; o0 += 32) {
-                    const uint32_t oj = o0 + lane;
-                    const uint32_t other = oj < re ? UD_AT(d.pool_hub, base + oj, d.pool_cap, 2) : 0xffffffffu;
-                    for (int k = 0; k < 32; ++k) rank += (__shfl_sync(FULL, other, k) < key) ? 1u : 0u;
-                }
+                for (int k = 0; k < 32; ++k) rank += (__shfl_sync(FULL, key, k) < key) ? 1u : 0u;
                 if (mine) {
                     fin_hub[fo + rs + rank] = key - gb;
                     fin_dist[fo + rs + rank] = dist;
                 }
+            } else {
+                // a long run: its hubs lie in one batch's id range [lo, lo + B),
+                // so a B-bit bitmap of the run (shared memory) and the prefix
+                // popcounts of its words give each entry its rank
+                const uint32_t lo = gb + batch * d.B, words = (d.B + 31) / 32;
+                for (uint32_t x = lane; x < words; x += 32) bm[x] = 0;
+                __syncwarp();
+                for (uint32_t c0 = rs; c0 < re; c0 += 32) {
+                    const uint32_t j = c0 + lane;
+                    if (j < re) {
+                        const uint32_t idx = UD_AT(d.pool_hub, base + j, d.pool_cap, 2) - lo;
+                        atomicOr(&bm[idx >> 5], 1u << (idx & 31));
+                    }
+                }
+                __syncwarp();
+                // exclusive prefix of the words' popcounts (lane i: words i, i + 32)
+                const uint32_t p0 = lane < (int)words ? __popc(bm[lane]) : 0u;
+                const uint32_t p1 = lane + 32 < (int)words ? __popc(bm[lane + 32]) : 0u;
+                uint32_t s0 = p0, s1 = p1;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y0 = __shfl_up_sync(FULL, s0, o), y1 = __shfl_up_sync(FULL, s1, o);
+                    if (lane >= o) {
+                        s0 += y0;
+                        s1 += y1;
+                    }
+                }
+                const uint32_t t0 = __shfl_sync(FULL, s0, 31);
+                if (lane < (int)words) pre[lane] = s0 - p0;
+                if (lane + 32 < (int)words) pre[lane + 32] = t0 + s1 - p1;
+                __syncwarp();
+                for (uint32_t c0 = rs; c0 < re; c0 += 32) {
+                    const uint32_t j = c0 + lane;
+                    if (j < re) {
+                        const uint32_t key = UD_AT(d.pool_hub, base + j, d.pool_cap, 2);
+                        const uint8_t dist = UD_AT(d.pool_dist, base + j, d.pool_cap, 2);
+                        const uint32_t idx = key - lo;
+                        const uint32_t rank = pre[idx >> 5] + __popc(bm[idx >> 5] & ((1u << (idx & 31)) - 1u));
+                        fin_hub[fo + rs + rank] = key - gb;
+                        fin_dist[fo + rs + rank] = dist;
+                    }
+                }
+                __syncwarp();
             }
             rs = re;
         }
