@@ -25,7 +25,7 @@ DEBUG = os.environ.get("PADO_DEBUG_BOUNDS", "") not in ("", "0")
 BUILD = PKG / ("_build_debug" if DEBUG else "_build")
 LIB = PKG / ("libpado_gpu_debug.so" if DEBUG else "libpado_gpu.so")
 SOURCES = ["capi.cu", "query.cu", "bp.cu", "unw.cu", "unw_many.cu", "weighted.cu", "profile.cu", "noalloc.cu",
-           "serve.cu", "ingest.cu", "selftest.cu"]
+           "serve.cu", "ingest.cu", "selftest.cu", "hostcopy.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

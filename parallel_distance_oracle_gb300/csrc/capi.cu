@@ -288,53 +288,8 @@ void build_ingested(pado_index *h, pado::IngestResult &r, uint32_t K, uint32_t B
     label_into(h, hg, g, h->K, B, s, phase);
 }
 
-// The device alias of page-locked host memory (cudaHostAlloc /
-// cudaHostRegister), which kernels may write directly; null for any other
-// pointer.
-void *mapped_host(void *p)
-{
-    if (!p) return nullptr;
-    cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();  // an unknown pointer is not an error here
-        return nullptr;
-    }
-    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
-}
-
-// Device-to-host copy by the SMs into page-locked memory (through its device
-// alias): 16 bytes per thread step, the unaligned head and tail bytewise.
-__global__ void __launch_bounds__(256) host_write_kernel(const unsigned char *src, unsigned char *dst, uint64_t bytes)
-{
-    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    const uint64_t nth = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t mis = (16 - ((uintptr_t)dst & 15)) & 15;
-    const uint64_t head = ((uintptr_t)src & 15) == ((uintptr_t)dst & 15) ? (mis < bytes ? mis : bytes) : bytes;
-    for (uint64_t i = tid; i < head; i += nth) dst[i] = src[i];
-    if (head == bytes) return;
-    const uint64_t body = (bytes - head) / 16;
-    const uint4 *s4 = reinterpret_cast<const uint4 *>(src + head);
-    uint4 *d4 = reinterpret_cast<uint4 *>(dst + head);
-    for (uint64_t i = tid; i < body; i += nth) d4[i] = s4[i];
-    for (uint64_t i = head + body * 16 + tid; i < bytes; i += nth) dst[i] = src[i];
-}
-
-// Copies `bytes` of device memory to host memory `h`: a page-locked
-// destination is written by the SMs (host_write_kernel), anything else by the
-// copy engines (cudaMemcpyAsync).  Kernel writes keep exports fast on hosts
-// where the copy engines are slowed by other work.
-void download_bytes(void *h, const void *d, uint64_t bytes, cudaStream_t s)
-{
-    if (!bytes) return;
-    unsigned char *dh = static_cast<unsigned char *>(mapped_host(h));
-    if (!dh) {
-        PADO_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, s));
-        return;
-    }
-    PADO_LAUNCH("host_write_kernel", s,
-                host_write_kernel<<<pado::grid_for(bytes / 16 + 1, 256, 152u * 16u), 256, 0, s>>>(
-                    static_cast<const unsigned char *>(d), dh, bytes));
-}
+using pado::download_bytes;
+using pado::mapped_host;
 
 // Export in original-id order: vertex v takes the list (and BP row) of rank[v].
 __global__ void __launch_bounds__(256) export_permute_kernel(uint32_t n, uint32_t K, int bp, const uint32_t *rank,

@@ -997,10 +997,11 @@ DevGraph prepare_csr(uint32_t n, const uint64_t *off, const uint32_t *adj, const
         if (w) g.w.alloc(std::max<uint64_t>(m, 1));
     }
     HostPhase ph("csr upload+check");
-    g.adj.upload(adj, m, s);
-    if (w) g.w.upload(w, m, s);
+    // page-locked inputs are read by the SMs, others go through the copy engines
+    upload_bytes(g.adj.p, adj, m * 4, s);
+    if (w) upload_bytes(g.w.p, w, m, s);
     PBuf<uint64_t> off64((uint64_t)n + 1, s);
-    PADO_CUDA(cudaMemcpyAsync(off64.p, off, ((uint64_t)n + 1) * 8, cudaMemcpyHostToDevice, s));
+    upload_bytes(off64.p, off, ((uint64_t)n + 1) * 8, s);
     PBuf<uint32_t> flags(1, s);
     flags.zero();
     PADO_LAUNCH("csr_check_kernel", s,
@@ -1009,7 +1010,7 @@ DevGraph prepare_csr(uint32_t n, const uint64_t *off, const uint32_t *adj, const
                                                                                      g.off.p, flags.p));
     if (rank) {
         rank_out->alloc(std::max<uint32_t>(n, 1));
-        rank_out->upload(rank, n, s);
+        upload_bytes(rank_out->p, rank, (uint64_t)n * 4, s);
         PBuf<uint32_t> seen(std::max<uint32_t>(n, 1), s);
         seen.zero();
         if (n)

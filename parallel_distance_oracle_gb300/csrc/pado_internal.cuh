@@ -175,6 +175,13 @@ uint64_t edge_bound_for_text(uint64_t bytes);
 uint64_t text_piece_bytes(uint64_t dflt);
 EdgeTextParser read_edge_file(const char *path, bool weighted, cudaStream_t s);
 
+// hostcopy.cu: the device alias of page-locked host memory (null for any other
+// pointer), and copies between host and device memory that the SMs carry out
+// when the host side is page-locked (the copy engines otherwise), enqueued on s.
+void *mapped_host(const void *p);
+void download_bytes(void *h, const void *d, uint64_t bytes, cudaStream_t s);
+void upload_bytes(void *d, const void *h, uint64_t bytes, cudaStream_t s);
+
 // capi.cu: the calling thread's last-error message, and read-only access to
 // an index handle, for entry points defined in other files.
 int set_error(int code, const std::string &msg);
