@@ -88,7 +88,8 @@ struct WDev {
     uint32_t *last_min[2];
     uint32_t *act_stamp[2];  // by round parity: round id at which the vertex accepted roots
     uint32_t *tail_stamp;
-    int16_t *snap;       // [B][B] rows of vertices < B at round start (batch 0)
+    int16_t *snap;       // [B][B] batch 0's temporary tables at round start, transposed:
+                         // snap[r * B + c] = vd[c][r] (root r of vertex c)
     uint32_t *status;
     unsigned long long *work;
 };
@@ -202,11 +203,16 @@ __global__ void __launch_bounds__(256) w_mark_kernel(WDev d, const uint32_t *fro
     w_mark_phase(d, front, *front_cnt, lid_cur, tails, tails_cnt);
 }
 
+// Snapshot of batch 0's temporary tables (vertices c < rows) for check (2),
+// stored transposed so that the lanes of a warp, each checking its own
+// candidate c against the same temporary root r, read one row of it.
 __device__ void w_snap_phase(const WDev &d, uint32_t rows)
 {
-    const uint64_t tot = (uint64_t)rows * d.B;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tot; i += (uint64_t)gridDim.x * blockDim.x)
-        d.snap[i] = d.vd[i];
+    const uint64_t tot = (uint64_t)d.B * d.B;
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < tot; j += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = j / d.B, c = j - r * d.B;
+        if (c < rows) d.snap[j] = d.vd[c * d.B + r];
+    }
 }
 
 __global__ void w_snap_kernel(WDev d, uint32_t rows) { w_snap_phase(d, rows); }
@@ -352,7 +358,7 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
             // covering label in that order, as the reference's loop does
             if (b == 0) {
                 bool look2 = r == INT_MIN;
-                const int16_t *crow = d.snap + (uint64_t)c * B;
+                const int16_t *ccol = d.snap + c;  // column c of the transposed snapshot
                 const uint16_t *tqp = d.vq + (uint64_t)t * B;
                 const int16_t *trow = d.vd + (uint64_t)t * B;
                 for (uint32_t k0 = 0; k0 < vql && __any_sync(FULL, look2); k0 += 32) {
@@ -370,7 +376,8 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
                         if (look2) {
 #pragma unroll
                             for (int u = 0; u < 4; ++u)
-                                sk[u] = (k + u < kn && s + rk[u] < creal) ? (int32_t)crow[rk[u]] : (int32_t)I16_INF;
+                                sk[u] = (k + u < kn && s + rk[u] < creal) ? (int32_t)ccol[(uint64_t)rk[u] * B]
+                                                                          : (int32_t)I16_INF;
 #pragma unroll
                             for (int u = 0; u < 4; ++u) {
                                 if (look2 && sk[u] != I16_INF) {
@@ -974,7 +981,7 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
                 PADO_CUDA(cudaMemsetAsync(&log_top.p[lid_cur & 1], 0, 8, s));
                 if (b == 0) {
                     PADO_LAUNCH("w_snap_kernel", s,
-                                w_snap_kernel<<<grid_for((uint64_t)nr * B, 256), 256, 0, s>>>(d, nr));
+                                w_snap_kernel<<<grid_for((uint64_t)B * B, 256), 256, 0, s>>>(d, nr));
                 }
                 PADO_LAUNCH("w_mark_kernel", s,
                             w_mark_kernel<<<grid_for((uint64_t)fsize * 32, 256), 256, 0, s>>>(d, fronts[cur], c_front[cur], lid_cur,
