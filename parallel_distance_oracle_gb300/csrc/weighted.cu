@@ -88,8 +88,7 @@ struct WDev {
     uint32_t *last_min[2];
     uint32_t *act_stamp[2];  // by round parity: round id at which the vertex accepted roots
     uint32_t *tail_stamp;
-    int16_t *snap;       // [B][B] batch 0's temporary tables at round start, transposed:
-                         // snap[r * B + c] = vd[c][r] (root r of vertex c)
+    int16_t *snap;       // [B][B] rows of vertices < B at round start (batch 0)
     uint32_t *status;
     unsigned long long *work;
 };
@@ -203,16 +202,11 @@ __global__ void __launch_bounds__(256) w_mark_kernel(WDev d, const uint32_t *fro
     w_mark_phase(d, front, *front_cnt, lid_cur, tails, tails_cnt);
 }
 
-// Snapshot of batch 0's temporary tables (vertices c < rows) for check (2),
-// stored transposed so that the lanes of a warp, each checking its own
-// candidate c against the same temporary root r, read one row of it.
 __device__ void w_snap_phase(const WDev &d, uint32_t rows)
 {
-    const uint64_t tot = (uint64_t)d.B * d.B;
-    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < tot; j += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t r = j / d.B, c = j - r * d.B;
-        if (c < rows) d.snap[j] = d.vd[c * d.B + r];
-    }
+    const uint64_t tot = (uint64_t)rows * d.B;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tot; i += (uint64_t)gridDim.x * blockDim.x)
+        d.snap[i] = d.vd[i];
 }
 
 __global__ void w_snap_kernel(WDev d, uint32_t rows) { w_snap_phase(d, rows); }
@@ -221,6 +215,48 @@ __global__ void w_snap_kernel(WDev d, uint32_t rows) { w_snap_phase(d, rows); }
 // Run by blocks of WPULL_WARPS warps.
 // tq: the round's work counter for dynamic tail claiming (null: static
 // grid-stride assignment).
+// One chunk of an in-order covering walk (checks (1) and (2) of the pull):
+// lane l holds list entry l of the chunk (`in`: the entry exists) with row
+// index `key`, order key `kcmp` and distance `el`.  Each pending lane j (bit j
+// of `pend`) has candidate root c_j, round minimum m_j and dists row
+// base + c_j * stride; the first entry with kcmp < s + c_j whose row value is
+// not INF and whose 16-bit sum with el is <= m_j covers it: lane j's r takes
+// that sum and bit j leaves the returned mask.  Four candidates are gathered
+// per step so that four loads are in flight.
+__device__ __forceinline__ uint32_t cover_chunk(uint32_t pend, bool in, uint32_t key, uint32_t kcmp, int32_t el,
+                                                const int16_t *base, uint64_t stride, uint32_t c, int32_t m,
+                                                uint32_t s, int32_t &r)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t todo = pend;
+    while (todo) {
+        int jj[4];
+        int32_t mm[4], sk[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            jj[u] = todo ? __ffs(todo) - 1 : -1;
+            todo &= todo - 1;  // (0 stays 0)
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t cu = __shfl_sync(FULL, c, jj[u] & 31);
+            mm[u] = __shfl_sync(FULL, m, jj[u] & 31);
+            sk[u] = (jj[u] >= 0 && in && kcmp < s + cu) ? (int32_t)base[(uint64_t)cu * stride + key] : (int32_t)I16_INF;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int32_t val = (int16_t)(el + sk[u]);
+            const uint32_t cov = __ballot_sync(FULL, sk[u] != I16_INF && val <= mm[u]);
+            if (cov) {
+                const int32_t v = __shfl_sync(FULL, val, __ffs(cov) - 1);
+                if (lane == jj[u]) r = v;
+                pend &= ~(1u << jj[u]);
+            }
+        }
+    }
+    return pend;
+}
+
 __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt, uint32_t s, uint32_t b,
                              uint32_t lid_cur, uint32_t *front_next, uint32_t *front_next_cnt, uint32_t *news,
                              uint32_t *news_cnt, uint32_t *retry, uint32_t *retry_cnt, unsigned char *wsm,
@@ -308,10 +344,13 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
         for (uint32_t i0 = 0; i0 < ntouch; i0 += 32) {
             const uint32_t i = i0 + lane;
             bool acc = false, isnew = false;
-            // check (1), warp-uniform over t's committed labels: a chunk of 32
-            // (hub, distance) pairs is loaded once and broadcast by shuffles,
-            // and each lane still looking gathers 4 buffer entries at a time,
-            // taking the first covering label in list order as the reference.
+            // checks (1) and (2) walk a list in order and stop at its first
+            // covering entry, as the reference's loops do.  The lanes hold 32
+            // consecutive entries of the list; the candidates still looking
+            // (bits of `pend`, one per lane of this group) are taken 4 at a
+            // time, each gathering its own row at the 32 entries' keys, and a
+            // ballot gives the first covering entry of each.  A candidate
+            // leaves the walk at the chunk that covers it.
             uint32_t c = 0, creal = 0;
             int32_t m = 0, r = INT_MAX;  // INT_MAX: not a candidate
             if (i < ntouch) {
@@ -320,76 +359,26 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
                 creal = s + c;
                 if (m < dt_get(d, t, c, stamp)) r = INT_MIN;  // accepted unless pruned below
             }
-            const int16_t *brow = d.buf + (uint64_t)c * d.n;
-            bool look = r == INT_MIN;
-            for (uint32_t j0 = 0; j0 < clen && __any_sync(FULL, look); j0 += 32) {
-                const uint32_t jn = min(32u, clen - j0);
-                const uint32_t hl = lane < (int)jn ? d.pool_hub[cbase + j0 + lane] : 0xffffffffu;
-                const int32_t dl = lane < (int)jn ? (int32_t)d.pool_dist[cbase + j0 + lane] : 0;
-                for (uint32_t k = 0; k < jn; k += 4) {
-                    uint32_t hk[4];
-                    int32_t dk[4], bk[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        hk[u] = __shfl_sync(FULL, hl, (int)(k + u) & 31);
-                        dk[u] = __shfl_sync(FULL, dl, (int)(k + u) & 31);
-                    }
-                    if (look) {
-#pragma unroll
-                        for (int u = 0; u < 4; ++u)
-                            bk[u] = (k + u < jn && hk[u] < creal) ? (int32_t)brow[hk[u]] : (int32_t)I16_INF;
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            if (look && bk[u] != I16_INF) {
-                                const int32_t val = (int16_t)(dk[u] + bk[u]);
-                                if (val <= m) {
-                                    r = val;
-                                    look = false;
-                                }
-                            }
-                        }
-                    }
-                }
+            uint32_t pend = __ballot_sync(FULL, r == INT_MIN);
+            // check (1): t's committed labels (hub, distance) against the
+            // candidate roots' dists_table rows (buf[c][hub])
+            for (uint32_t j0 = 0; j0 < clen && pend; j0 += 32) {
+                const bool in = j0 + lane < clen;
+                const uint32_t hl = in ? d.pool_hub[cbase + j0 + lane] : 0xffffffffu;
+                const int32_t dl = in ? (int32_t)d.pool_dist[cbase + j0 + lane] : 0;
+                pend = cover_chunk(pend, in, hl, hl, dl, d.buf, d.n, c, m, s, r);
             }
-            // check (2) (batch 0 only), warp-uniform over t's temporary labels
-            // in first-acceptance order: a chunk of 32 (root, distance) pairs
-            // is loaded once and broadcast by shuffles, each lane still
-            // looking gathers 4 snapshot entries at a time and takes the first
-            // covering label in that order, as the reference's loop does
+            // check (2) (batch 0 only): t's temporary labels in acceptance
+            // order (root, distance) against the snapshot rows of the
+            // candidates' temporary tables, roots before the candidate only
             if (b == 0) {
-                bool look2 = r == INT_MIN;
-                const int16_t *ccol = d.snap + c;  // column c of the transposed snapshot
                 const uint16_t *tqp = d.vq + (uint64_t)t * B;
                 const int16_t *trow = d.vd + (uint64_t)t * B;
-                for (uint32_t k0 = 0; k0 < vql && __any_sync(FULL, look2); k0 += 32) {
-                    const uint32_t kn = min(32u, vql - k0);
-                    const uint32_t rl = lane < (int)kn ? (uint32_t)tqp[k0 + lane] : 0u;
-                    const int32_t tl = lane < (int)kn ? (int32_t)trow[rl] : 0;
-                    for (uint32_t k = 0; k < kn; k += 4) {
-                        uint32_t rk[4];
-                        int32_t tk[4], sk[4];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            rk[u] = __shfl_sync(FULL, rl, (int)(k + u) & 31);
-                            tk[u] = __shfl_sync(FULL, tl, (int)(k + u) & 31);
-                        }
-                        if (look2) {
-#pragma unroll
-                            for (int u = 0; u < 4; ++u)
-                                sk[u] = (k + u < kn && s + rk[u] < creal) ? (int32_t)ccol[(uint64_t)rk[u] * B]
-                                                                          : (int32_t)I16_INF;
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                if (look2 && sk[u] != I16_INF) {
-                                    const int32_t val = (int16_t)(tk[u] + sk[u]);
-                                    if (val <= m) {
-                                        r = val;
-                                        look2 = false;
-                                    }
-                                }
-                            }
-                        }
-                    }
+                for (uint32_t k0 = 0; k0 < vql && pend; k0 += 32) {
+                    const bool in = k0 + lane < vql;
+                    const uint32_t rl = in ? (uint32_t)tqp[k0 + lane] : 0u;
+                    const int32_t tl = in ? (int32_t)trow[rl] : 0;
+                    pend = cover_chunk(pend, in, rl, s + rl, tl, d.snap, B, c, m, s, r);
                 }
             }
             if (i < ntouch) {
@@ -981,7 +970,7 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
                 PADO_CUDA(cudaMemsetAsync(&log_top.p[lid_cur & 1], 0, 8, s));
                 if (b == 0) {
                     PADO_LAUNCH("w_snap_kernel", s,
-                                w_snap_kernel<<<grid_for((uint64_t)B * B, 256), 256, 0, s>>>(d, nr));
+                                w_snap_kernel<<<grid_for((uint64_t)nr * B, 256), 256, 0, s>>>(d, nr));
                 }
                 PADO_LAUNCH("w_mark_kernel", s,
                             w_mark_kernel<<<grid_for((uint64_t)fsize * 32, 256), 256, 0, s>>>(d, fronts[cur], c_front[cur], lid_cur,
