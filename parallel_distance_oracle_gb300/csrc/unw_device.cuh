@@ -882,12 +882,14 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             for (; j < len && cnt + 32 <= (uint32_t)SMALL_CAP; j += 32) {
                 const uint32_t jj = j + lane;
                 const bool in = jj < len;
+                // hub and distance are independent loads: one round trip
                 const uint8_t dd = in ? UD_AT(d.pool_dist, base + jj, d.pool_cap, 2) : (uint8_t)U8_INF;
+                const uint32_t hb = in ? UD_AT(d.pool_hub, base + jj, d.pool_cap, 2) : 0u;
                 const bool sm = in && dd < iter;
                 const uint32_t m = __ballot_sync(FULL, sm);
                 if (sm) {
                     const uint32_t p = cnt + __popc(m & ((1u << lane) - 1u));
-                    wr.sh[p] = UD_AT(d.pool_hub, base + jj, d.pool_cap, 2);
+                    wr.sh[p] = hb;
                     wr.sd[p] = (uint8_t)(iter - dd);  // slack: covered iff d(r, h) <= slack
                 }
                 cnt += __popc(m);
