@@ -136,8 +136,32 @@ __device__ __forceinline__ bool warp_reserve_w(const WDev &d, uint32_t v, uint32
 }
 
 // initialize_tables (pado_weighted_unv_unp.h:281-330)
+// A head h of round lid - 1 whose smallest accepted root is mn: its
+// neighbours t > mn become tails of round lid (stamp lid), once each.  The
+// adjacency is in descending order, so the walk stops at the first t <= mn.
+// Called by one whole warp.
+__device__ __forceinline__ void w_mark_head(const WDev &d, uint32_t h, uint32_t mn, uint32_t lid, uint32_t *tails,
+                                            uint32_t *tails_cnt)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t e_end = d.off[h + 1];
+    for (uint32_t e0 = d.off[h]; e0 < e_end; e0 += 32) {
+        const uint32_t e = e0 + lane;
+        const bool in = e < e_end;
+        const uint32_t t = in ? d.adj[e] : 0u;
+        const bool ok = in && t > mn;
+        if (ok && d.tail_stamp[t] != lid) {
+            if (atomicExch(&d.tail_stamp[t], lid) != lid) tails[agg_append(tails_cnt)] = t;
+        }
+        if (__ballot_sync(FULL, in && !ok)) break;
+    }
+}
+
+// front: the batch roots as the heads of the first round (host-driven loop);
+// with `tails` instead, the roots mark the first round's tails themselves.
 __device__ void w_root_init_phase(const WDev &d, uint32_t s, uint32_t nroots, uint32_t lid0, uint32_t *front,
-                                  uint32_t *front_cnt, uint32_t *news, uint32_t *news_cnt)
+                                  uint32_t *front_cnt, uint32_t *news, uint32_t *news_cnt, uint32_t *tails = nullptr,
+                                  uint32_t *tails_cnt = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -160,9 +184,10 @@ __device__ void w_root_init_phase(const WDev &d, uint32_t s, uint32_t nroots, ui
             d.last_cnt[p][r] = 1;
             d.last_min[p][r] = r;
             d.act_stamp[p][r] = lid0;
-            front[atomicAdd(front_cnt, 1u)] = r;
+            if (front) front[atomicAdd(front_cnt, 1u)] = r;
             news[atomicAdd(news_cnt, 1u)] = r;
         }
+        if (tails) w_mark_head(d, r, r, lid0 + 1, tails, tails_cnt);
     }
 }
 
@@ -176,23 +201,11 @@ __global__ void __launch_bounds__(256) w_root_init_kernel(WDev d, uint32_t s, ui
 __device__ void w_mark_phase(const WDev &d, const uint32_t *front, uint32_t cnt, uint32_t lid_cur, uint32_t *tails,
                              uint32_t *tails_cnt)
 {
-    const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const int pp = (lid_cur - 1) & 1;
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < cnt; q += nw) {
         const uint32_t h = front[q];
-        const uint32_t mn = d.last_min[pp][h];
-        const uint32_t e_end = d.off[h + 1];
-        for (uint32_t e0 = d.off[h]; e0 < e_end; e0 += 32) {
-            const uint32_t e = e0 + lane;
-            const bool in = e < e_end;
-            const uint32_t t = in ? d.adj[e] : 0u;
-            const bool ok = in && t > mn;
-            if (ok && d.tail_stamp[t] != lid_cur) {
-                if (atomicExch(&d.tail_stamp[t], lid_cur) != lid_cur) tails[agg_append(tails_cnt)] = t;
-            }
-            if (__ballot_sync(FULL, in && !ok)) break;
-        }
+        w_mark_head(d, h, d.last_min[pp][h], lid_cur, tails, tails_cnt);
     }
 }
 
@@ -211,10 +224,6 @@ __device__ void w_snap_phase(const WDev &d, uint32_t rows)
 
 __global__ void w_snap_kernel(WDev d, uint32_t rows) { w_snap_phase(d, rows); }
 
-// Per-warp dynamic shared memory: rmin[B] int32, res[B] int32, touched[B] u16.
-// Run by blocks of WPULL_WARPS warps.
-// tq: the round's work counter for dynamic tail claiming (null: static
-// grid-stride assignment).
 // One chunk of an in-order covering walk (checks (1) and (2) of the pull):
 // lane l holds list entry l of the chunk (`in`: the entry exists) with row
 // index `key`, order key `kcmp` and distance `el`.  Each pending lane j (bit j
@@ -257,10 +266,16 @@ __device__ __forceinline__ uint32_t cover_chunk(uint32_t pend, bool in, uint32_t
     return pend;
 }
 
+// The pull of one round (send_messages, pado_weighted_unv_unp.h:409-870, as
+// a pull).  Per-warp dynamic shared memory: rmin[B] int32, res[B] int32,
+// touched[B] u16.  Run by blocks of WPULL_WARPS warps.
+// tq: the round's work counter for dynamic tail claiming (null: static
+// grid-stride assignment).  front_next (may be null) collects the next round's
+// heads; next_tails (may be null) collects the next round's tails directly.
 __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt, uint32_t s, uint32_t b,
                              uint32_t lid_cur, uint32_t *front_next, uint32_t *front_next_cnt, uint32_t *news,
                              uint32_t *news_cnt, uint32_t *retry, uint32_t *retry_cnt, unsigned char *wsm,
-                             uint32_t *tq = nullptr)
+                             uint32_t *tq = nullptr, uint32_t *next_tails = nullptr, uint32_t *next_tails_cnt = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
@@ -455,10 +470,13 @@ __device__ void w_pull_phase(const WDev &d, const uint32_t *tails, uint32_t cnt,
                 d.last_cnt[cp][t] = nacc;
                 d.last_min[cp][t] = mnacc;
                 d.act_stamp[cp][t] = lid_cur;
-                front_next[atomicAdd(front_next_cnt, 1u)] = t;
+                if (front_next) front_next[atomicAdd(front_next_cnt, 1u)] = t;
             }
         }
         __syncwarp();
+        // t is a head of the next round: with next_tails it marks that
+        // round's tails itself (no separate mark phase)
+        if (nacc && next_tails) w_mark_head(d, t, mnacc, lid_cur + 1, next_tails, next_tails_cnt);
     };
     if (tq) {
         // dynamic claiming: the next claim is issued before the current tail
@@ -633,17 +651,20 @@ __global__ void __launch_bounds__(256) w_compact_kernel(WDev d, const uint64_t *
 enum WPhase : uint32_t { WP_START = 0, WP_ROUND = 1, WP_PULL_RETRY = 2, WP_END = 3, WP_COMMIT_RETRY = 4, WP_DONE = 5 };
 enum WExit : uint32_t { WX_RUNNING = 0, WX_DONE = 1, WX_NEED_LOG = 2, WX_NEED_POOL = 3, WX_STALL = 4 };
 
+// Round lid reads tails[lid % 3] and appends the next round's tails to
+// tails[(lid + 1) % 3] as its heads accept; the leader clears the third slot
+// for the round after.
 struct WLoopCtl {
     GridBar bar;
-    uint32_t phase, b, lid, cur;      // resume point: phase, batch, last stamp, front parity
+    uint32_t phase, b, lid;           // resume point: phase, batch, last stamp
     uint32_t rounds, levels;
-    uint32_t front_cnt[2], tails_cnt[2], news_cnt[2];
-    uint32_t tq[2];                   // the pull's work counter, by the round's tails slot
+    uint32_t tails_cnt[3], news_cnt[2];
+    uint32_t tq[3];                   // the pull's work counter, by the round's tails slot
     uint32_t rr_cnt, retry_cnt, status, exit_code;
 };
 
 struct WLoopBufs {
-    uint32_t *front[2], *tails[2], *news[2];  // news by batch parity
+    uint32_t *tails[3], *news[2];  // news by batch parity
     uint32_t *rr, *retry;
     uint32_t nbatches;
 };
@@ -652,14 +673,13 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
 {
     extern __shared__ __align__(16) unsigned char wsm[];
     const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
-    uint32_t phase = vload(&c->phase), b = vload(&c->b), lid = vload(&c->lid), cur = vload(&c->cur);
+    uint32_t phase = vload(&c->phase), b = vload(&c->b), lid = vload(&c->lid);
     uint32_t rounds = vload(&c->rounds), levels = vload(&c->levels);
     auto save = [&](uint32_t ph, uint32_t ex) {
         if (leader) {
             c->phase = ph;
             c->b = b;
             c->lid = lid;
-            c->cur = cur;
             c->rounds = rounds;
             c->levels = levels;
             c->exit_code = ex;
@@ -673,13 +693,15 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
             }
             const uint32_t s = b * d.B, nr = min(d.B, d.n - s);
             const uint32_t lid0 = lid + 1;
-            cur = lid0 & 1;
-            // front[cur], news[b & 1] and log[lid0 & 1] were cleared at the end of the previous batch
-            w_root_init_phase(d, s, nr, lid0, bf.front[cur], &c->front_cnt[cur], bf.news[b & 1],
-                              &c->news_cnt[b & 1]);
+            // news[b & 1], log[lid0 & 1] and the first round's tails slot
+            // were cleared at the end of the previous batch; the roots mark
+            // the first round's tails
+            w_root_init_phase(d, s, nr, lid0, nullptr, nullptr, bf.news[b & 1], &c->news_cnt[b & 1],
+                              bf.tails[(lid0 + 1) % 3], &c->tails_cnt[(lid0 + 1) % 3]);
             if (leader) {
-                c->tails_cnt[(lid0 + 1) & 1] = 0;  // the first round's tails
-                c->tq[(lid0 + 1) & 1] = 0;
+                c->tails_cnt[(lid0 + 2) % 3] = 0;  // filled by the first round
+                c->tq[(lid0 + 2) % 3] = 0;
+                d.log_top[(lid0 + 1) & 1] = 0;     // the first round's log
             }
             if (!grid_barrier(&c->bar, &c->status)) return;
             lid = lid0;
@@ -689,24 +711,26 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
         }
         if (phase == WP_ROUND || phase == WP_PULL_RETRY) {
             const uint32_t s = b * d.B, nr = min(d.B, d.n - s);
-            const uint32_t lid_cur = lid + 1, nxt = cur ^ 1, tp = lid_cur & 1;
+            const uint32_t lid_cur = lid + 1, tp = lid_cur % 3, tn = (lid_cur + 1) % 3;
             if (phase == WP_ROUND) {
                 // Bellman-Ford rounds are bounded by the vertex count
                 if (rounds > d.n + 2) {
                     save(WP_DONE, WX_STALL);
                     return;
                 }
-                if (b == 0) w_snap_phase(d, nr);
-                w_mark_phase(d, bf.front[cur], vload(&c->front_cnt[cur]), lid_cur, bf.tails[tp], &c->tails_cnt[tp]);
-                if (leader) d.log_top[lid_cur & 1] = 0;  // last read by the pull of lid_cur - 1
-                if (!grid_barrier(&c->bar, &c->status)) return;
+                if (b == 0) {
+                    // check (2) reads the batch's temporary tables as of the round start
+                    w_snap_phase(d, nr);
+                    if (!grid_barrier(&c->bar, &c->status)) return;
+                }
             }
-            w_pull_phase(d, bf.tails[tp], vload(&c->tails_cnt[tp]), s, b, lid_cur, bf.front[nxt], &c->front_cnt[nxt],
-                         bf.news[b & 1], &c->news_cnt[b & 1], bf.retry, &c->retry_cnt, wsm, &c->tq[tp]);
+            w_pull_phase(d, bf.tails[tp], vload(&c->tails_cnt[tp]), s, b, lid_cur, nullptr, nullptr, bf.news[b & 1],
+                         &c->news_cnt[b & 1], bf.retry, &c->retry_cnt, wsm, &c->tq[tp], bf.tails[tn],
+                         &c->tails_cnt[tn]);
             if (leader) {
-                c->front_cnt[cur] = 0;             // consumed by this round's mark
-                c->tails_cnt[(lid_cur + 1) & 1] = 0;  // read by the previous round's pull
-                c->tq[(lid_cur + 1) & 1] = 0;
+                c->tails_cnt[(lid_cur + 2) % 3] = 0;  // read by the previous round's pull
+                c->tq[(lid_cur + 2) % 3] = 0;
+                d.log_top[(lid_cur + 1) & 1] = 0;     // the next round's log, last read by this pull
             }
             if (!grid_barrier(&c->bar, &c->status)) return;
             if (vload(&c->retry_cnt)) {
@@ -716,9 +740,7 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
             ++levels;
             ++rounds;
             lid = lid_cur;
-            const uint32_t fsize = vload(&c->front_cnt[nxt]);
-            cur = nxt;
-            phase = fsize ? WP_ROUND : WP_END;
+            phase = vload(&c->tails_cnt[tn]) ? WP_ROUND : WP_END;
             continue;
         }
         if (phase == WP_END || phase == WP_COMMIT_RETRY) {
@@ -730,6 +752,8 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
                 if (leader) {
                     d.log_top[(lid + 1) & 1] = 0;  // the next batch's root log (read by the last pull)
                     c->news_cnt[nb ^ 1] = 0;       // the next batch's new-label list
+                    c->tails_cnt[(lid + 2) % 3] = 0;  // the next batch's first tails
+                    c->tq[(lid + 2) % 3] = 0;
                 }
                 if (!grid_barrier(&c->bar, &c->status)) return;
                 w_commit_phase(d, bf.news[nb], nn, s, bf.retry, &c->retry_cnt);
@@ -893,9 +917,9 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
         PADO_CHECK(nbatches < 65535u, PADO_E_ARG, "more than 65534 batches");
         if (!host_loop && n) {
             DBuf<WLoopCtl> ctl(1);
-            DBuf<uint32_t> tails2(n), news2(n), rr(n);
+            DBuf<uint32_t> tails2(n), tails3(n), news2(n), rr(n);
             ctl.fill_bytes(0, s);
-            WLoopBufs bf{{front0.p, front1.p}, {tails.p, tails2.p}, {news.p, news2.p}, rr.p, retry.p, nbatches};
+            WLoopBufs bf{{tails.p, tails2.p, tails3.p}, {news.p, news2.p}, rr.p, retry.p, nbatches};
             const void *kfn = (const void *)w_loop_kernel;
             PADO_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pull_smem));
             int dev = 0, sms = 0, per_sm = 0;
@@ -925,12 +949,12 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
                     unsigned long long lt[2];
                     PADO_CUDA(cudaMemcpy(lt, log_top.p, 16, cudaMemcpyDeviceToHost));
                     grow_logs(lt[(h.lid + 1) & 1]);
-                    // the failed tails become the whole tail list of the round
-                    const uint32_t tp = (h.lid + 1) & 1;
-                    uint32_t *tl[2] = {tails.p, tails2.p};
-                    PADO_CUDA(cudaMemcpyAsync(tl[tp], retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
+                    // the failed tails become the whole tail list of the round;
+                    // the next round's tails marked so far stay
+                    const uint32_t tp = (h.lid + 1) % 3;
+                    PADO_CUDA(cudaMemcpyAsync(bf.tails[tp], retry.p, h.retry_cnt * 4ull, cudaMemcpyDeviceToDevice, s));
                     h.tails_cnt[tp] = h.retry_cnt;
-                    h.tq[0] = h.tq[1] = 0;  // the re-run pull claims from zero
+                    h.tq[tp] = 0;  // the re-run pull claims from zero
                 } else {
                     PADO_CHECK(h.exit_code == WX_NEED_POOL, PADO_E_STATE, "weighted labeling loop stopped unexpectedly");
                     unsigned long long top = 0;
