@@ -157,6 +157,17 @@ __device__ __forceinline__ void w_mark_head(const WDev &d, uint32_t h, uint32_t 
     }
 }
 
+// The temporary rows of the B vertices from s on (a batch's roots), back to
+// INF (the rows are contiguous).
+__device__ void w_rows_clear_phase(const WDev &d, uint32_t s)
+{
+    const uint32_t rows = min(d.B, d.n - s);
+    const uint64_t tot = (uint64_t)rows * d.B;
+    int16_t *p = d.vd + (uint64_t)s * d.B;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tot; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = I16_INF;
+}
+
 // front: the batch roots as the heads of the first round (host-driven loop);
 // with `tails` instead, the roots mark the first round's tails themselves.
 __device__ void w_root_init_phase(const WDev &d, uint32_t s, uint32_t nroots, uint32_t lid0, uint32_t *front,
@@ -507,39 +518,145 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_pull_kernel(WDev d, con
                  wsm);
 }
 
-// filter_out_labels (pado_weighted_unv_unp.h:1052-1184) on pre-filter values;
-// a filtered entry gets bit 15 of its vq slot set.
-__device__ void w_filter_phase(const WDev &d, const uint32_t *news, uint32_t nnews, uint32_t s)
+// filter_out_labels (pado_weighted_unv_unp.h:1052-1184) on pre-filter values
+// for the temporary labels i0 .. i0 + 31 of v (one per lane): label c is
+// dropped, by setting bit 15 of its vq slot, when some root r < c of v's list
+// has d(v, r) <= d(v, c), d(c, r) <= d(v, c) and d(v, r) + d(c, r) <= d(v, c),
+// d(c, r) read from root c's temporary row.  v's list is taken 32 entries at
+// a time into the lanes and broadcast; each lane still looking keeps four
+// root-row gathers in flight.  Bit 15 is masked off wherever a slot is read,
+// so chunks of one v may run in different warps at once.
+__device__ __forceinline__ void w_filter_chunk(const WDev &d, uint32_t v, uint32_t L, uint32_t i0, uint32_t s)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t B = d.B;
+    uint16_t *vq = d.vq + (uint64_t)v * B;
+    const int16_t *row = d.vd + (uint64_t)v * B;
+    const uint32_t i = i0 + lane;
+    const bool valid = i < L;
+    uint32_t c = 0;
+    int32_t dvc = 0;
+    if (valid) {
+        c = vq[i] & 0x7fffu;
+        dvc = row[c];
+    }
+    const int16_t *crow = d.vd + (uint64_t)(s + c) * B;
+    bool filt = false;
+    for (uint32_t k0 = 0; k0 < L && __any_sync(FULL, valid && !filt); k0 += 32) {
+        const uint32_t kn = min(32u, L - k0);
+        const uint32_t rl = (uint32_t)lane < kn ? (uint32_t)(vq[k0 + lane] & 0x7fffu) : 0u;
+        const int32_t dl = (uint32_t)lane < kn ? (int32_t)row[rl] : 0;
+        for (uint32_t k = 0; k < kn; k += 4) {
+            uint32_t ru[4];
+            int32_t du[4], gu[4];
+            bool pu[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                ru[u] = __shfl_sync(FULL, rl, (int)(k + u) & 31);
+                du[u] = __shfl_sync(FULL, dl, (int)(k + u) & 31);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                pu[u] = valid && !filt && k + u < kn && ru[u] < c && du[u] <= dvc;
+                gu[u] = pu[u] ? (int32_t)crow[ru[u]] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (pu[u] && gu[u] <= dvc && du[u] + gu[u] <= dvc) filt = true;
+        }
+    }
+    __syncwarp();
+    if (valid && filt) vq[i] |= 0x8000u;
+    __syncwarp();
+}
+
+// update_index (pado_weighted_unv_unp.h:913-950) for one vertex v: append the
+// unfiltered temporary labels in ascending root order, then clear v's
+// temporary row unless `keep_row` (a batch root's row, which other vertices'
+// filters still read; it is cleared when the next batch starts).
+__device__ __forceinline__ void w_commit_one(const WDev &d, uint32_t v, uint32_t s, uint32_t *retry,
+                                             uint32_t *retry_cnt, bool keep_row)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t B = d.B;
+    const uint32_t L = d.vq_len[v];
+    uint16_t *vq = d.vq + (uint64_t)v * B;
+    int16_t *row = d.vd + (uint64_t)v * B;
+    uint32_t keep = 0;
+    for (uint32_t i = lane; i < L; i += 32) keep += (vq[i] & 0x8000u) ? 0u : 1u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) keep += __shfl_xor_sync(FULL, keep, o);
+    const uint32_t len = d.lab_len[v];
+    uint64_t base;
+    if (keep && !warp_reserve_w(d, v, len + keep, base, lane)) {
+        if (lane == 0) {
+            atomicOr(d.status, ST_POOL_RETRY);
+            retry[atomicAdd(retry_cnt, 1u)] = v;
+        }
+        return;
+    }
+    if (keep) {
+        for (uint32_t i0 = 0; i0 < L; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool mine = i < L && !(vq[i] & 0x8000u);
+            const uint32_t key = mine ? vq[i] : 0xffffffffu;
+            uint32_t rank = 0;
+            for (uint32_t o0 = 0; o0 < L; o0 += 32) {
+                const uint32_t oj = o0 + lane;
+                const uint32_t other = (oj < L && !(vq[oj] & 0x8000u)) ? (uint32_t)vq[oj] : 0xffffffffu;
+                for (int k = 0; k < 32; ++k) rank += (__shfl_sync(FULL, other, k) < key) ? 1u : 0u;
+            }
+            if (mine) {
+                d.pool_hub[base + len + rank] = s + key;
+                d.pool_dist[base + len + rank] = row[key];
+            }
+        }
+    }
+    __syncwarp();
+    if (!keep_row)
+        for (uint32_t i = lane; i < L; i += 32) row[vq[i] & 0x7fffu] = I16_INF;
+    __syncwarp();
+    if (lane == 0) {
+        d.lab_len[v] = len + keep;
+        d.vq_len[v] = 0;
+    }
+}
+
+// Filter of a batch's new-label vertices, a warp per vertex.  With `heavy`,
+// a warp filters only the first 32 labels of its vertex and lists the
+// vertices with more, whose other chunks w_filter_heavy_phase spreads over the
+// grid; with `commit`, each warp commits its vertex right after filtering it
+// (roots' rows kept, see w_commit_one).
+__device__ void w_filter_phase(const WDev &d, const uint32_t *news, uint32_t nnews, uint32_t s,
+                               uint32_t *heavy = nullptr, uint32_t *heavy_cnt = nullptr, bool commit = false,
+                               uint32_t nroots = 0, uint32_t *retry = nullptr, uint32_t *retry_cnt = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t B = d.B;
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nnews; q += nw) {
         const uint32_t v = news[q];
         const uint32_t L = d.vq_len[v];
-        uint16_t *vq = d.vq + (uint64_t)v * B;
-        const int16_t *row = d.vd + (uint64_t)v * B;
-        for (uint32_t i0 = 0; i0 < L; i0 += 32) {
-            const uint32_t i = i0 + lane;
-            bool filt = false;
-            if (i < L) {
-                const uint32_t c = vq[i] & 0x7fffu;
-                const int32_t dvc = row[c];
-                const int16_t *crow = d.vd + (uint64_t)(s + c) * B;
-                for (uint32_t k = 0; k < L && !filt; ++k) {
-                    const uint32_t r = vq[k] & 0x7fffu;
-                    if (c <= r) continue;
-                    const int32_t dvr = row[r];
-                    if (dvr > dvc) continue;
-                    const int32_t dcr = crow[r];
-                    if (dcr > dvc) continue;
-                    if (dvr + dcr <= dvc) filt = true;
-                }
-            }
-            __syncwarp();
-            if (filt) vq[i] |= 0x8000u;
-            __syncwarp();
+        if (heavy) {
+            w_filter_chunk(d, v, L, 0, s);
+            if (L > 32 && lane == 0) heavy[atomicAdd(heavy_cnt, 1u)] = v;
+        } else {
+            for (uint32_t i0 = 0; i0 < L; i0 += 32) w_filter_chunk(d, v, L, i0, s);
         }
+        if (commit) w_commit_one(d, v, s, retry, retry_cnt, v >= s && v - s < nroots);
+    }
+}
+
+// The chunks after the first of the listed vertices, one (vertex, chunk) item
+// per warp: item j is chunk 1 + j / nheavy of vertex heavy[j % nheavy].
+__device__ void w_filter_heavy_phase(const WDev &d, const uint32_t *heavy, uint32_t nheavy, uint32_t s)
+{
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint64_t items = (uint64_t)nheavy * ((d.B + 31) / 32 - 1);
+    for (uint64_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < items; j += nw) {
+        const uint32_t v = heavy[j % nheavy];
+        const uint32_t i0 = 32u * (uint32_t)(1 + j / nheavy);
+        const uint32_t L = d.vq_len[v];
+        if (i0 < L) w_filter_chunk(d, v, L, i0, s);
     }
 }
 
@@ -568,56 +685,14 @@ __global__ void __launch_bounds__(256) w_buf_reset_kernel(WDev d, uint32_t s, ui
     w_buf_reset_phase(d, s, nroots);
 }
 
-// update_index (pado_weighted_unv_unp.h:913-950): append the unfiltered
-// temporary labels in ascending root order, then clear the temporary rows.
+// update_index (pado_weighted_unv_unp.h:913-950) for a list of vertices.
 __device__ void w_commit_phase(const WDev &d, const uint32_t *news, uint32_t nnews, uint32_t s, uint32_t *retry,
-                               uint32_t *retry_cnt)
+                               uint32_t *retry_cnt, uint32_t nroots = 0)
 {
-    const int lane = threadIdx.x & 31;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t B = d.B;
     for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nnews; q += nw) {
         const uint32_t v = news[q];
-        const uint32_t L = d.vq_len[v];
-        uint16_t *vq = d.vq + (uint64_t)v * B;
-        int16_t *row = d.vd + (uint64_t)v * B;
-        uint32_t keep = 0;
-        for (uint32_t i = lane; i < L; i += 32) keep += (vq[i] & 0x8000u) ? 0u : 1u;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) keep += __shfl_xor_sync(FULL, keep, o);
-        const uint32_t len = d.lab_len[v];
-        uint64_t base;
-        if (keep && !warp_reserve_w(d, v, len + keep, base, lane)) {
-            if (lane == 0) {
-                atomicOr(d.status, ST_POOL_RETRY);
-                retry[atomicAdd(retry_cnt, 1u)] = v;
-            }
-            continue;
-        }
-        if (keep) {
-            for (uint32_t i0 = 0; i0 < L; i0 += 32) {
-                const uint32_t i = i0 + lane;
-                const bool mine = i < L && !(vq[i] & 0x8000u);
-                const uint32_t key = mine ? vq[i] : 0xffffffffu;
-                uint32_t rank = 0;
-                for (uint32_t o0 = 0; o0 < L; o0 += 32) {
-                    const uint32_t oj = o0 + lane;
-                    const uint32_t other = (oj < L && !(vq[oj] & 0x8000u)) ? (uint32_t)vq[oj] : 0xffffffffu;
-                    for (int k = 0; k < 32; ++k) rank += (__shfl_sync(FULL, other, k) < key) ? 1u : 0u;
-                }
-                if (mine) {
-                    d.pool_hub[base + len + rank] = s + key;
-                    d.pool_dist[base + len + rank] = row[key];
-                }
-            }
-        }
-        __syncwarp();
-        for (uint32_t i = lane; i < L; i += 32) row[vq[i] & 0x7fffu] = I16_INF;
-        __syncwarp();
-        if (lane == 0) {
-            d.lab_len[v] = len + keep;
-            d.vq_len[v] = 0;
-        }
+        w_commit_one(d, v, s, retry, retry_cnt, v >= s && v - s < nroots);
     }
 }
 
@@ -660,12 +735,13 @@ struct WLoopCtl {
     uint32_t rounds, levels;
     uint32_t tails_cnt[3], news_cnt[2];
     uint32_t tq[3];                   // the pull's work counter, by the round's tails slot
+    uint32_t heavy_cnt;               // batch 0's vertices with more than 32 temporary labels
     uint32_t rr_cnt, retry_cnt, status, exit_code;
 };
 
 struct WLoopBufs {
     uint32_t *tails[3], *news[2];  // news by batch parity
-    uint32_t *rr, *retry;
+    uint32_t *rr, *retry, *heavy;
     uint32_t nbatches;
 };
 
@@ -696,6 +772,7 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
             // news[b & 1], log[lid0 & 1] and the first round's tails slot
             // were cleared at the end of the previous batch; the roots mark
             // the first round's tails
+            if (b > 0) w_rows_clear_phase(d, s - d.B);  // the previous batch's roots' temporary rows
             w_root_init_phase(d, s, nr, lid0, nullptr, nullptr, bf.news[b & 1], &c->news_cnt[b & 1],
                               bf.tails[(lid0 + 1) % 3], &c->tails_cnt[(lid0 + 1) % 3]);
             if (leader) {
@@ -747,16 +824,29 @@ __global__ void __launch_bounds__(WPULL_WARPS * 32, 8) w_loop_kernel(WDev d, WLo
             const uint32_t s = b * d.B, nr = min(d.B, d.n - s), nb = b & 1;
             if (phase == WP_END) {
                 const uint32_t nn = vload(&c->news_cnt[nb]);
-                w_filter_phase(d, bf.news[nb], nn, s);
-                w_buf_reset_phase(d, s, nr);
                 if (leader) {
                     d.log_top[(lid + 1) & 1] = 0;  // the next batch's root log (read by the last pull)
                     c->news_cnt[nb ^ 1] = 0;       // the next batch's new-label list
                     c->tails_cnt[(lid + 2) % 3] = 0;  // the next batch's first tails
                     c->tq[(lid + 2) % 3] = 0;
                 }
-                if (!grid_barrier(&c->bar, &c->status)) return;
-                w_commit_phase(d, bf.news[nb], nn, s, bf.retry, &c->retry_cnt);
+                if (b == 0) {
+                    // batch 0 has vertices with hundreds of temporary labels:
+                    // their chunks after the first are spread over the grid,
+                    // and the commit follows once every filter is done
+                    w_filter_phase(d, bf.news[nb], nn, s, bf.heavy, &c->heavy_cnt);
+                    if (!grid_barrier(&c->bar, &c->status)) return;
+                    w_filter_heavy_phase(d, bf.heavy, vload(&c->heavy_cnt), s);
+                    w_buf_reset_phase(d, s, nr);
+                    if (!grid_barrier(&c->bar, &c->status)) return;
+                    w_commit_phase(d, bf.news[nb], nn, s, bf.retry, &c->retry_cnt);
+                } else {
+                    // filter and commit each vertex in one go; the roots'
+                    // rows, read by other vertices' filters, are cleared when
+                    // the next batch starts
+                    w_filter_phase(d, bf.news[nb], nn, s, nullptr, nullptr, true, nr, bf.retry, &c->retry_cnt);
+                    w_buf_reset_phase(d, s, nr);
+                }
             } else {
                 w_commit_phase(d, bf.rr, vload(&c->rr_cnt), s, bf.retry, &c->retry_cnt);
             }
@@ -917,9 +1007,9 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
         PADO_CHECK(nbatches < 65535u, PADO_E_ARG, "more than 65534 batches");
         if (!host_loop && n) {
             DBuf<WLoopCtl> ctl(1);
-            DBuf<uint32_t> tails2(n), tails3(n), news2(n), rr(n);
+            DBuf<uint32_t> tails2(n), tails3(n), news2(n), rr(n), heavy(n);
             ctl.fill_bytes(0, s);
-            WLoopBufs bf{{tails.p, tails2.p, tails3.p}, {news.p, news2.p}, rr.p, retry.p, nbatches};
+            WLoopBufs bf{{tails.p, tails2.p, tails3.p}, {news.p, news2.p}, rr.p, retry.p, heavy.p, nbatches};
             const void *kfn = (const void *)w_loop_kernel;
             PADO_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pull_smem));
             int dev = 0, sms = 0, per_sm = 0;
