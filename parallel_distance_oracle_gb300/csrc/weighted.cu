@@ -32,22 +32,27 @@
 // exactly this schedule (the oracle's snapshot mode) produced byte-identical
 // label sets to the reference on every graph it was compared on.
 //
-// Device mapping: as in the unweighted labeler -- a mark kernel stamps the
-// tails of the active heads, and a pull kernel runs a warp per tail that owns
-// the tail's rows of dists_table / temporary labels for the round: it min-
-// reduces the incoming relaxations per root in shared memory, runs checks (1)
-// and (2) lane-per-candidate, and commits.  The previous round's accepted
-// (root, distance) pairs of each vertex are read from a parity-double-
-// buffered log, so heads can be read while their owners accept new roots.
-// dists_table entries carry a batch stamp and never need resetting.
+// Device mapping: as in the unweighted labeler -- the tails of the active
+// heads are stamped and listed, and a pull runs a warp per tail that owns the
+// tail's rows of dists_table / temporary labels for the round: it min-reduces
+// the incoming relaxations per root in shared memory, walks checks (1) and (2)
+// per candidate (list entries across the lanes, a ballot for the first
+// covering entry), and commits.  The previous round's accepted (root,
+// distance) pairs of each vertex are read from a parity-double-buffered log,
+// so heads can be read while their owners accept new roots.  dists_table
+// entries carry a batch stamp and never need resetting.
 //
 // Schedule: one persistent cooperative launch (w_loop_kernel) runs every
-// batch -- start (root tables), rounds (mark, then pull), end (filter and
-// buffer reset, then commit) -- with a bounded grid barrier between phases
-// instead of a kernel launch and a host round trip each.  It returns to the
-// host only to grow the round logs or the label pool (the failed tails or
-// vertices are re-run exactly afterwards) or on an error.  PADO_LEVEL_LOOP=host
-// selects the host-driven loop of separate kernels instead.
+// batch with a bounded grid barrier between phases instead of a kernel launch
+// and a host round trip each: start (the previous batch's roots' temporary
+// rows cleared; root tables; the roots mark the first round's tails), one
+// phase per round (the pull; a tail that accepts marks the next round's tails
+// itself; batch 0 takes a snapshot phase first), end (later batches: filter
+// and commit each vertex in one phase; batch 0: filter, then the long lists'
+// remaining chunks over the grid, then commit).  It returns to the host only
+// to grow the round logs or the label pool (the failed tails or vertices are
+// re-run exactly afterwards) or on an error.  PADO_LEVEL_LOOP=host selects the
+// host-driven loop of separate kernels (mark, pull, filter, commit) instead.
 
 #include <algorithm>
 #include <climits>
