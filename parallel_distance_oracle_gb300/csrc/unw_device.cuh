@@ -17,6 +17,10 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int SMALL_CAP = 384;                 // labels with d < iter staged in smem per chunk
+// distance test of a light tail: staged lists at least this long, tested
+// against at most this many candidates, are walked per candidate with the
+// entries across the lanes instead of a lane per candidate
+constexpr uint32_t WALK_MIN_STAGED = 64, WALK_MAX_CANDIDATES = 16;
 constexpr uint32_t HEAVY_DEG = 2048;           // tails this large are processed by a block
 
 // A vertex's label group of one level: list position, size and the level id
@@ -910,7 +914,42 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             const uint8_t *row = bc.dm + (uint64_t)idx * bc.dn - bc.base;  // row[h] for a hub h of this graph
             if (!whole && c0 > 0) next = stage(0);
             for (;;) {
-                if (keep) {
+                const uint32_t nk = __popc(__ballot_sync(FULL, keep));
+                if (nst >= WALK_MIN_STAGED && nk <= WALK_MAX_CANDIDATES) {
+                    // few candidates against a long staged list: each pending
+                    // candidate walks the list with 32 entries across the
+                    // lanes (a ballot per candidate and chunk), four
+                    // candidates' gathers in flight per step
+                    uint32_t pend = __ballot_sync(FULL, keep);
+                    const uint64_t rl = (uint64_t)bc.base + bc.dn;
+                    for (uint32_t k0 = 0; k0 < nst && pend; k0 += 32) {
+                        const bool in = k0 + lane < nst;
+                        const uint32_t hl = in ? wr.sh[k0 + lane] : 0xffffffffu;
+                        const uint32_t sl = in ? (uint32_t)wr.sd[k0 + lane] : 0u;
+                        uint32_t todo = pend;
+                        while (todo) {
+                            int jj[4];
+                            uint32_t vv[4];
+                            bool ok[4];
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                jj[u] = todo ? __ffs(todo) - 1 : -1;
+                                todo &= todo - 1;  // (0 stays 0)
+                            }
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                const uint32_t ix = __shfl_sync(FULL, (uint32_t)idx, jj[u] & 31);
+                                const uint8_t *rw = bc.dm + (uint64_t)ix * bc.dn - bc.base;
+                                ok[u] = jj[u] >= 0 && in && hl < s + ix;
+                                vv[u] = ok[u] ? (uint32_t)UD_AT(rw, hl, rl, 4) : 255u;
+                            }
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                if (__ballot_sync(FULL, ok[u] && vv[u] <= sl)) pend &= ~(1u << jj[u]);
+                        }
+                    }
+                    keep = keep && ((pend >> lane) & 1u);
+                } else if (keep) {
                     uint32_t k = 0;
                     // four dist_matrix gathers in flight per lane
                     for (; k + 4 <= nst; k += 4) {
