@@ -19,8 +19,10 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int SMALL_CAP = 384;                 // labels with d < iter staged in smem per chunk
 // distance test of a light tail: staged lists at least this long, tested
 // against at most this many candidates, are walked per candidate with the
-// entries across the lanes instead of a lane per candidate
-constexpr uint32_t WALK_MIN_STAGED = 64, WALK_MAX_CANDIDATES = 16;
+// entries across the lanes instead of a lane per candidate (R-MAT s20:
+// 64 / 16 gave 155.5 ms per build, 16 / 32 153.7 ms; 32 graphs of up to 60k
+// vertices: 0.422 and 0.354 s, against 0.497 s with lanes per candidate only)
+constexpr uint32_t WALK_MIN_STAGED = 16, WALK_MAX_CANDIDATES = 32;
 constexpr uint32_t HEAVY_DEG = 2048;           // tails this large are processed by a block
 
 // A vertex's label group of one level: list position, size and the level id
@@ -916,10 +918,11 @@ __device__ void pull_light_tail(const UnwDev &d, const PullArgs &a, uint32_t t, 
             for (;;) {
                 const uint32_t nk = __popc(__ballot_sync(FULL, keep));
                 if (nst >= WALK_MIN_STAGED && nk <= WALK_MAX_CANDIDATES) {
-                    // few candidates against a long staged list: each pending
-                    // candidate walks the list with 32 entries across the
+                    // a staged list of WALK_MIN_STAGED or more entries: each
+                    // pending candidate walks it with 32 entries across the
                     // lanes (a ballot per candidate and chunk), four
-                    // candidates' gathers in flight per step
+                    // candidates' gathers in flight per step; a candidate
+                    // leaves at the chunk that covers it
                     uint32_t pend = __ballot_sync(FULL, keep);
                     const uint64_t rl = (uint64_t)bc.base + bc.dn;
                     for (uint32_t k0 = 0; k0 < nst && pend; k0 += 32) {
