@@ -21,7 +21,8 @@ constexpr int SMALL_CAP = 384;                 // labels with d < iter staged in
 // against at most this many candidates, are walked per candidate with the
 // entries across the lanes instead of a lane per candidate (R-MAT s20:
 // 64 / 16 gave 155.5 ms per build, 16 / 32 153.7 ms; 32 graphs of up to 60k
-// vertices: 0.422 and 0.354 s, against 0.497 s with lanes per candidate only)
+// vertices: 0.422 and 0.354 s, against 0.497 s with lanes per candidate only;
+// walking every staged list, 1 / 32, was 152.7 ms against 151.8 ms for 16 / 32)
 constexpr uint32_t WALK_MIN_STAGED = 16, WALK_MAX_CANDIDATES = 32;
 constexpr uint32_t HEAVY_DEG = 2048;           // tails this large are processed by a block
 
