@@ -94,6 +94,9 @@ struct WDev {
     uint32_t *act_stamp[2];  // by round parity: round id at which the vertex accepted roots
     uint32_t *tail_stamp;
     int16_t *snap;       // [B][B] rows of vertices < B at round start (batch 0)
+    uint64_t *rbase;     // [B] pool position of root c's labels when its buf row was filled
+    uint32_t *rlen;      // [B] their count (the row's reset reads these, not the live list,
+                         // which a commit in the same phase may extend or move)
     uint32_t *status;
     unsigned long long *work;
 };
@@ -140,7 +143,6 @@ __device__ __forceinline__ bool warp_reserve_w(const WDev &d, uint32_t v, uint32
     return true;
 }
 
-// initialize_tables (pado_weighted_unv_unp.h:281-330)
 // A head h of round lid - 1 whose smallest accepted root is mn: its
 // neighbours t > mn become tails of round lid (stamp lid), once each.  The
 // adjacency is in descending order, so the walk stops at the first t <= mn.
@@ -173,6 +175,7 @@ __device__ void w_rows_clear_phase(const WDev &d, uint32_t s)
         p[i] = I16_INF;
 }
 
+// initialize_tables (pado_weighted_unv_unp.h:281-330).
 // front: the batch roots as the heads of the first round (host-driven loop);
 // with `tails` instead, the roots mark the first round's tails themselves.
 __device__ void w_root_init_phase(const WDev &d, uint32_t s, uint32_t nroots, uint32_t lid0, uint32_t *front,
@@ -190,6 +193,8 @@ __device__ void w_root_init_phase(const WDev &d, uint32_t s, uint32_t nroots, ui
         for (uint32_t j = lane; j < len; j += 32) row[d.pool_hub[base + j]] = d.pool_dist[base + j];
         __syncwarp();
         if (lane == 0) {
+            d.rbase[c] = base;
+            d.rlen[c] = len;
             row[r] = 0;
             d.vq[(uint64_t)r * d.B] = (uint16_t)c;
             d.vq_len[r] = 1;
@@ -670,7 +675,9 @@ __global__ void __launch_bounds__(256) w_filter_kernel(WDev d, const uint32_t *n
     w_filter_phase(d, news, nnews, s);
 }
 
-// reset_tables for the roots' buffer rows (pado_weighted_unv_unp.h:872-891).
+// reset_tables for the roots' buffer rows (pado_weighted_unv_unp.h:872-891):
+// the entries the root init set, from the label list as it was then (a list
+// slot keeps its first entries when the list grows or moves).
 __device__ void w_buf_reset_phase(const WDev &d, uint32_t s, uint32_t nroots)
 {
     const int lane = threadIdx.x & 31;
@@ -678,8 +685,8 @@ __device__ void w_buf_reset_phase(const WDev &d, uint32_t s, uint32_t nroots)
     for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nroots; c += nw) {
         const uint32_t r = s + c;
         int16_t *row = d.buf + (uint64_t)c * d.n;
-        const uint64_t base = d.lab_off[r];
-        const uint32_t len = d.lab_len[r];
+        const uint64_t base = d.rbase[c];
+        const uint32_t len = d.rlen[c];
         for (uint32_t j = lane; j < len; j += 32) row[d.pool_hub[base + j]] = I16_INF;
         if (lane == 0) row[r] = I16_INF;
     }
@@ -887,6 +894,8 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
     DBuf<uint32_t> lab_len(n), lab_cap(n), last_cnt0(n), last_cnt1(n), last_min0(n), last_min1(n);
     DBuf<uint32_t> act_stamp0(n), act_stamp1(n), tail_stamp(n), vq_len(n);
     DBuf<int16_t> buf((uint64_t)B * n), vd((uint64_t)n * B), snap((uint64_t)B * B);
+    DBuf<uint64_t> rbase(B);
+    DBuf<uint32_t> rlen(B);
     DBuf<uint16_t> vq((uint64_t)n * B);
     DBuf<uint32_t> dt((uint64_t)n * B);
     DBuf<uint32_t> log0(lcap), log1(lcap);
@@ -949,6 +958,8 @@ LabelRun w_label(const DevGraph &g, uint32_t B, LabelStore &out, cudaStream_t s)
     d.act_stamp[0] = act_stamp0.p;
     d.act_stamp[1] = act_stamp1.p;
     d.tail_stamp = tail_stamp.p;
+    d.rbase = rbase.p;
+    d.rlen = rlen.p;
     d.snap = snap.p;
     d.status = status.p;
     d.work = work_counters();
